@@ -1,0 +1,448 @@
+// Elementwise kernels of the generic time-stepping path: each reference broadcast group
+// of a substep (src/timesteppers.jl) becomes one pass over HBM, plus dealias!, the
+// spectral helpers of the Diffusion module and the Parseval reductions.
+//
+// Arithmetic follows the reference broadcasts' evaluation order so that FP64 results
+// agree with the CPU restatement to rounding.
+#include <mutex>
+#include <vector>
+
+#include "ff_common.cuh"
+
+namespace ff {
+
+// per-mode coefficient (see ff_coef); the kind is uniform across the launch
+template <typename T> struct Coef {
+  const void* p;
+  int kind;
+  T re, im;
+  __device__ __forceinline__ cx<T> mul(cx<T> v, int64_t i) const {
+    switch (kind) {
+      case FF_COEF_REAL: return scl(v, static_cast<const T*>(p)[i]);
+      case FF_COEF_COMPLEX: return cmul(static_cast<const cx<T>*>(p)[i], v);
+      case FF_COEF_SCALAR: return im == T(0) ? scl(v, re) : cmul(mk<T>(re, im), v);
+      default: return czero<T>();
+    }
+  }
+};
+
+template <typename T> static Coef<T> coef(const ff_coef& c) {
+  Coef<T> r;
+  r.p = c.ptr;
+  r.kind = c.kind;
+  r.re = (T)c.re;
+  r.im = (T)c.im;
+  return r;
+}
+
+static int check_coef(const ff_coef& c, const char* what) {
+  FF_CHECK_ARG(c.kind >= FF_COEF_NONE && c.kind <= FF_COEF_SCALAR, "%s: bad coefficient kind %d", what, c.kind);
+  FF_CHECK_ARG(!(c.kind == FF_COEF_REAL || c.kind == FF_COEF_COMPLEX) || c.ptr != nullptr,
+               "%s: coefficient array is null", what);
+  return FF_OK;
+}
+
+#define GRID_STRIDE(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+template <typename T>
+__global__ void k_euler(int64_t n, cx<T>* sol, const cx<T>* __restrict__ N, Coef<T> L, T dt, const T* filter) {
+  GRID_STRIDE(i, n) {
+    const cx<T> s = sol[i];
+    cx<T> v;
+    if (filter) v = scl(add(s, scl(add(N[i], L.mul(s, i)), dt)), filter[i]);
+    else v = add(s, scl(add(L.mul(s, i), N[i]), dt));
+    sol[i] = v;
+  }
+}
+
+template <typename T>
+__global__ void k_rk4_substep(int64_t n, cx<T>* RHS, Coef<T> L, const cx<T>* x, const cx<T>* sol, cx<T>* newsol,
+                              T c) {
+  GRID_STRIDE(i, n) {
+    const cx<T> r = add(RHS[i], L.mul(x[i], i));
+    RHS[i] = r;
+    if (newsol) newsol[i] = add(sol[i], scl(r, c));
+  }
+}
+
+template <typename T>
+__global__ void k_rk4_update(int64_t n, cx<T>* sol, cx<T>* RHS4, Coef<T> L, const cx<T>* x, const cx<T>* R1,
+                             const cx<T>* R2, const cx<T>* R3, T c6, const T* filter) {
+  GRID_STRIDE(i, n) {
+    const cx<T> r4 = add(RHS4[i], L.mul(x[i], i));
+    RHS4[i] = r4;
+    const cx<T> acc = add(add(add(R1[i], scl(R2[i], T(2))), scl(R3[i], T(2))), r4);
+    cx<T> v = add(sol[i], scl(acc, c6));
+    if (filter) v = scl(v, filter[i]);
+    sol[i] = v;
+  }
+}
+
+template <typename T>
+__global__ void k_lsrk54(int64_t n, cx<T>* sol, cx<T>* RHS, cx<T>* S2, Coef<T> L, T A, T B, T dt, int first,
+                         const T* filter) {
+  GRID_STRIDE(i, n) {
+    const cx<T> s = sol[i];
+    const cx<T> r = add(RHS[i], L.mul(s, i));
+    RHS[i] = r;
+    const cx<T> q = first ? scl(r, dt) : add(scl(S2[i], A), scl(r, dt));
+    S2[i] = q;
+    cx<T> v = add(s, scl(q, B));
+    if (filter) v = scl(v, filter[i]);
+    sol[i] = v;
+  }
+}
+
+template <typename T>
+__global__ void k_etd12(int64_t n, cx<T>* out, Coef<T> eh, const cx<T>* sol, Coef<T> z, const cx<T>* N) {
+  GRID_STRIDE(i, n) out[i] = add(eh.mul(sol[i], i), z.mul(N[i], i));
+}
+
+template <typename T>
+__global__ void k_etd3(int64_t n, cx<T>* out, Coef<T> eh, const cx<T>* sol1, Coef<T> z, const cx<T>* N1,
+                       const cx<T>* N3) {
+  GRID_STRIDE(i, n) out[i] = add(eh.mul(sol1[i], i), z.mul(sub(scl(N3[i], T(2)), N1[i]), i));
+}
+
+template <typename T>
+__global__ void k_etd_update(int64_t n, cx<T>* sol, Coef<T> eL, Coef<T> a, Coef<T> b, Coef<T> g,
+                             const cx<T>* N1, const cx<T>* N2, const cx<T>* N3, const cx<T>* N4, const T* filter) {
+  GRID_STRIDE(i, n) {
+    // expL sol + alpha N1 + (2 beta)(N2 + N3) + Gamma N4
+    cx<T> v = add(eL.mul(sol[i], i), a.mul(N1[i], i));
+    v = add(v, scl(b.mul(add(N2[i], N3[i]), i), T(2)));
+    v = add(v, g.mul(N4[i], i));
+    if (filter) v = scl(v, filter[i]);
+    sol[i] = v;
+  }
+}
+
+template <typename T>
+__global__ void k_ab3(int64_t n, cx<T>* sol, cx<T>* RHS, cx<T>* Rm1, cx<T>* Rm2, Coef<T> L, T dt, int euler,
+                      T h1, T h2, T h3, const T* filter) {
+  GRID_STRIDE(i, n) {
+    const cx<T> s = sol[i];
+    const cx<T> r = add(RHS[i], L.mul(s, i));
+    RHS[i] = r;
+    const cx<T> m1 = Rm1[i];
+    cx<T> v;
+    if (euler) v = add(s, scl(r, dt));
+    else v = add(s, scl(add(sub(scl(r, h1), scl(m1, h2)), scl(Rm2[i], h3)), dt));
+    if (filter) v = scl(v, filter[i]);
+    sol[i] = v;
+    Rm2[i] = m1;
+    Rm1[i] = r;
+  }
+}
+
+template <typename T> __global__ void k_filter(int64_t n, cx<T>* sol, const T* __restrict__ f) {
+  GRID_STRIDE(i, n) sol[i] = scl(sol[i], f[i]);
+}
+
+template <typename T>
+__global__ void k_dealias(cx<T>* fh, int64_t d0, int64_t d1, int64_t d2, int64_t total, int64_t lo0, int64_t hi0,
+                          int64_t lo1, int64_t hi1, int64_t lo2, int64_t hi2) {
+  GRID_STRIDE(i, total) {
+    const int64_t i0 = i % d0;
+    const int64_t r = i / d0;
+    const int64_t i1 = r % d1;
+    const int64_t i2 = (r / d1) % d2;
+    if ((i0 >= lo0 && i0 < hi0) || (i1 >= lo1 && i1 < hi1) || (i2 >= lo2 && i2 < hi2)) fh[i] = czero<T>();
+  }
+}
+
+template <typename T>
+__global__ void k_mul_ik(int64_t n0, int64_t total, cx<T>* out, const cx<T>* in, const T* __restrict__ k) {
+  GRID_STRIDE(i, total) out[i] = mul_i(scl(in[i], k[i % n0]));
+}
+
+// u_hat = i l zeta_hat / K^2, v_hat = -i kr zeta_hat / K^2 (psi_hat = -zeta_hat / K^2)
+template <typename T>
+__global__ void k_velocities(int64_t nkr, int64_t n, const cx<T>* __restrict__ zh, const T* __restrict__ kr,
+                             const T* __restrict__ l, const T* __restrict__ invK, cx<T>* uh, cx<T>* vh) {
+  GRID_STRIDE(i, n) {
+    const cx<T> z = zh[i];
+    const int64_t c = i % nkr, j = i / nkr;
+    uh[i] = mul_i(scl(z, l[j] * invK[i]));
+    vh[i] = mul_mi(scl(z, kr[c] * invK[i]));
+  }
+}
+
+template <typename T> __global__ void k_real_mul(int64_t n, int64_t na, T* x, const T* __restrict__ a) {
+  GRID_STRIDE(i, n) x[i] *= a[i % na];
+}
+
+// ---- deterministic two-pass reduction ---------------------------------------------------
+// pass 1: each CTA writes one FP64 partial; pass 2: one CTA sums the partials in order.
+#define FF_RED_THREADS 256
+#define FF_RED_MAXBLOCKS 1024
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double sh[FF_RED_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  v = 0.0;
+  if (w == 0) {
+    v = l < (int)(blockDim.x >> 5) ? sh[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+
+// mode 0: |u|^2 [* wt]; mode 1: Re u.  rfft_form weights rows 1..n0-2 by 2.
+template <typename T>
+__global__ void k_parseval_partial(const cx<T>* __restrict__ uh, int64_t n0, int64_t total, int rfft_form, int mode,
+                                   const T* __restrict__ wt, double* partial) {
+  double acc = 0.0;
+  GRID_STRIDE(i, total) {
+    const cx<T> u = uh[i];
+    double v = mode == 0 ? (double)u.x * (double)u.x + (double)u.y * (double)u.y : (double)u.x;
+    if (wt) v *= (double)wt[i];
+    const int64_t i0 = i % n0;
+    const double w = (rfft_form && i0 > 0 && i0 < n0 - 1) ? 2.0 : 1.0;
+    acc += w * v;
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int n, double norm, double* out) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partial[i];
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) *out = acc * norm;
+}
+
+// per-device reduction scratch, allocated on first use and kept until exit
+static double* reduction_scratch() {
+  static std::mutex mu;
+  static std::vector<double*> bufs;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)bufs.size() <= dev) bufs.resize(dev + 1, nullptr);
+  if (!bufs[dev]) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, (FF_RED_MAXBLOCKS + 8) * sizeof(double)) != cudaSuccess) return nullptr;
+    bufs[dev] = (double*)p;
+  }
+  return bufs[dev];
+}
+
+template <typename T>
+static int parseval(const void* uh, int64_t n0, int64_t nrest, int rfft_form, int mode, double norm, double* out,
+                    cudaStream_t s, const void* wt = nullptr, double* dev_out = nullptr) {
+  const int64_t total = n0 * nrest;
+  double* scratch = reduction_scratch();
+  if (!scratch) {
+    set_error("parsevalsum: reduction scratch allocation failed");
+    return FF_ERR_ALLOC;
+  }
+  int blocks = elementwise_grid(total, FF_RED_THREADS);
+  if (blocks > FF_RED_MAXBLOCKS) blocks = FF_RED_MAXBLOCKS;
+  k_parseval_partial<T><<<blocks, FF_RED_THREADS, 0, s>>>((const cx<T>*)uh, n0, total, rfft_form, mode,
+                                                           (const T*)wt, scratch);
+  FF_LAUNCHED("k_parseval_partial");
+  double* res = dev_out ? dev_out : scratch + FF_RED_MAXBLOCKS;
+  k_sum_partials<<<1, FF_RED_THREADS, 0, s>>>(scratch, blocks, norm, res);
+  FF_LAUNCHED("k_sum_partials");
+  if (dev_out) return FF_OK;
+  FF_CUDA(cudaMemcpyAsync(out, res, sizeof(double), cudaMemcpyDeviceToHost, s));
+  FF_CUDA(cudaStreamSynchronize(s));
+  return FF_OK;
+}
+
+}  // namespace ff
+
+using namespace ff;
+
+#define FF_PREC_DISPATCH(prec, CALL_F64, CALL_F32)                      \
+  do {                                                                  \
+    FF_CHECK_ARG((prec) == FF_F64 || (prec) == FF_F32, "bad precision %d", (prec)); \
+    if ((prec) == FF_F64) { CALL_F64; } else { CALL_F32; }              \
+  } while (0)
+
+#define LAUNCH1D(kernel, n, ...)                                            \
+  do {                                                                      \
+    if ((n) <= 0) return FF_OK;                                             \
+    kernel<<<elementwise_grid((n), 256), 256, 0, (cudaStream_t)stream>>>(__VA_ARGS__); \
+    FF_LAUNCHED(#kernel);                                                   \
+  } while (0)
+
+extern "C" {
+
+int ff_euler_update(int prec, int64_t n, void* sol, const void* N, ff_coef L, double dt, const void* filter,
+                    void* stream) {
+  FF_CHECK_ARG(sol && N, "ff_euler_update: null array");
+  if (int st = check_coef(L, "ff_euler_update")) return st;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_euler<double>, n, n, (double2*)sol, (const double2*)N, coef<double>(L), dt, (const double*)filter),
+      LAUNCH1D(k_euler<float>, n, n, (float2*)sol, (const float2*)N, coef<float>(L), (float)dt, (const float*)filter));
+  return FF_OK;
+}
+
+int ff_rk4_substep(int prec, int64_t n, void* RHS, ff_coef L, const void* x, const void* sol, void* newsol, double c,
+                   void* stream) {
+  FF_CHECK_ARG(RHS && x && (!newsol || sol), "ff_rk4_substep: null array");
+  if (int st = check_coef(L, "ff_rk4_substep")) return st;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_rk4_substep<double>, n, n, (double2*)RHS, coef<double>(L), (const double2*)x, (const double2*)sol,
+               (double2*)newsol, c),
+      LAUNCH1D(k_rk4_substep<float>, n, n, (float2*)RHS, coef<float>(L), (const float2*)x, (const float2*)sol,
+               (float2*)newsol, (float)c));
+  return FF_OK;
+}
+
+int ff_rk4_update(int prec, int64_t n, void* sol, void* RHS4, ff_coef L, const void* x, const void* RHS1,
+                  const void* RHS2, const void* RHS3, double c6, const void* filter, void* stream) {
+  FF_CHECK_ARG(sol && RHS4 && x && RHS1 && RHS2 && RHS3, "ff_rk4_update: null array");
+  if (int st = check_coef(L, "ff_rk4_update")) return st;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_rk4_update<double>, n, n, (double2*)sol, (double2*)RHS4, coef<double>(L), (const double2*)x,
+               (const double2*)RHS1, (const double2*)RHS2, (const double2*)RHS3, c6, (const double*)filter),
+      LAUNCH1D(k_rk4_update<float>, n, n, (float2*)sol, (float2*)RHS4, coef<float>(L), (const float2*)x,
+               (const float2*)RHS1, (const float2*)RHS2, (const float2*)RHS3, (float)c6, (const float*)filter));
+  return FF_OK;
+}
+
+int ff_lsrk54_stage(int prec, int64_t n, void* sol, void* RHS, void* S2, ff_coef L, double A, double B, double dt,
+                    int first, const void* filter, void* stream) {
+  FF_CHECK_ARG(sol && RHS && S2, "ff_lsrk54_stage: null array");
+  if (int st = check_coef(L, "ff_lsrk54_stage")) return st;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_lsrk54<double>, n, n, (double2*)sol, (double2*)RHS, (double2*)S2, coef<double>(L), A, B, dt, first,
+               (const double*)filter),
+      LAUNCH1D(k_lsrk54<float>, n, n, (float2*)sol, (float2*)RHS, (float2*)S2, coef<float>(L), (float)A, (float)B,
+               (float)dt, first, (const float*)filter));
+  return FF_OK;
+}
+
+int ff_etdrk4_substep12(int prec, int64_t n, void* out, ff_coef e_half, const void* sol, ff_coef zeta,
+                        const void* N, void* stream) {
+  FF_CHECK_ARG(out && sol && N, "ff_etdrk4_substep12: null array");
+  if (int st = check_coef(e_half, "ff_etdrk4_substep12")) return st;
+  if (int st = check_coef(zeta, "ff_etdrk4_substep12")) return st;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_etd12<double>, n, n, (double2*)out, coef<double>(e_half), (const double2*)sol, coef<double>(zeta),
+               (const double2*)N),
+      LAUNCH1D(k_etd12<float>, n, n, (float2*)out, coef<float>(e_half), (const float2*)sol, coef<float>(zeta),
+               (const float2*)N));
+  return FF_OK;
+}
+
+int ff_etdrk4_substep3(int prec, int64_t n, void* out, ff_coef e_half, const void* sol1, ff_coef zeta,
+                       const void* N1, const void* N3, void* stream) {
+  FF_CHECK_ARG(out && sol1 && N1 && N3, "ff_etdrk4_substep3: null array");
+  if (int st = check_coef(e_half, "ff_etdrk4_substep3")) return st;
+  if (int st = check_coef(zeta, "ff_etdrk4_substep3")) return st;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_etd3<double>, n, n, (double2*)out, coef<double>(e_half), (const double2*)sol1, coef<double>(zeta),
+               (const double2*)N1, (const double2*)N3),
+      LAUNCH1D(k_etd3<float>, n, n, (float2*)out, coef<float>(e_half), (const float2*)sol1, coef<float>(zeta),
+               (const float2*)N1, (const float2*)N3));
+  return FF_OK;
+}
+
+int ff_etdrk4_update(int prec, int64_t n, void* sol, ff_coef expL, ff_coef alpha, ff_coef beta, ff_coef Gamma,
+                     const void* N1, const void* N2, const void* N3, const void* N4, const void* filter,
+                     void* stream) {
+  FF_CHECK_ARG(sol && N1 && N2 && N3 && N4, "ff_etdrk4_update: null array");
+  for (const ff_coef* c : {&expL, &alpha, &beta, &Gamma})
+    if (int st = check_coef(*c, "ff_etdrk4_update")) return st;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_etd_update<double>, n, n, (double2*)sol, coef<double>(expL), coef<double>(alpha), coef<double>(beta),
+               coef<double>(Gamma), (const double2*)N1, (const double2*)N2, (const double2*)N3, (const double2*)N4,
+               (const double*)filter),
+      LAUNCH1D(k_etd_update<float>, n, n, (float2*)sol, coef<float>(expL), coef<float>(alpha), coef<float>(beta),
+               coef<float>(Gamma), (const float2*)N1, (const float2*)N2, (const float2*)N3, (const float2*)N4,
+               (const float*)filter));
+  return FF_OK;
+}
+
+int ff_ab3_update(int prec, int64_t n, void* sol, void* RHS, void* RHSm1, void* RHSm2, ff_coef L, double dt,
+                  int euler, const void* filter, void* stream) {
+  FF_CHECK_ARG(sol && RHS && RHSm1 && RHSm2, "ff_ab3_update: null array");
+  if (int st = check_coef(L, "ff_ab3_update")) return st;
+  const double h1 = 23.0 / 12.0, h2 = 16.0 / 12.0, h3 = 5.0 / 12.0;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_ab3<double>, n, n, (double2*)sol, (double2*)RHS, (double2*)RHSm1, (double2*)RHSm2, coef<double>(L), dt,
+               euler, h1, h2, h3, (const double*)filter),
+      LAUNCH1D(k_ab3<float>, n, n, (float2*)sol, (float2*)RHS, (float2*)RHSm1, (float2*)RHSm2, coef<float>(L),
+               (float)dt, euler, (float)h1, (float)h2, (float)h3, (const float*)filter));
+  return FF_OK;
+}
+
+int ff_filter_mul(int prec, int64_t n, void* sol, const void* filter, void* stream) {
+  FF_CHECK_ARG(sol && filter, "ff_filter_mul: null array");
+  FF_PREC_DISPATCH(prec, LAUNCH1D(k_filter<double>, n, n, (double2*)sol, (const double*)filter),
+                   LAUNCH1D(k_filter<float>, n, n, (float2*)sol, (const float*)filter));
+  return FF_OK;
+}
+
+int ff_dealias(int prec, void* fh, const int64_t dims[4], const int64_t lo[3], const int64_t hi[3], void* stream) {
+  FF_CHECK_ARG(fh && dims && lo && hi, "ff_dealias: null argument");
+  for (int d = 0; d < 4; ++d) FF_CHECK_ARG(dims[d] >= 1, "ff_dealias: dims[%d] must be >= 1", d);
+  const int64_t total = dims[0] * dims[1] * dims[2] * dims[3];
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_dealias<double>, total, (double2*)fh, dims[0], dims[1], dims[2], total, lo[0], hi[0], lo[1], hi[1],
+               lo[2], hi[2]),
+      LAUNCH1D(k_dealias<float>, total, (float2*)fh, dims[0], dims[1], dims[2], total, lo[0], hi[0], lo[1], hi[1],
+               lo[2], hi[2]));
+  return FF_OK;
+}
+
+int ff_mul_ik(int prec, int64_t n0, int64_t nrest, void* out, const void* in, const void* k, void* stream) {
+  FF_CHECK_ARG(out && in && k && n0 >= 1 && nrest >= 1, "ff_mul_ik: bad argument");
+  const int64_t total = n0 * nrest;
+  FF_PREC_DISPATCH(prec, LAUNCH1D(k_mul_ik<double>, total, n0, total, (double2*)out, (const double2*)in, (const double*)k),
+                   LAUNCH1D(k_mul_ik<float>, total, n0, total, (float2*)out, (const float2*)in, (const float*)k));
+  return FF_OK;
+}
+
+int ff_real_mul(int prec, int64_t n, int64_t na, void* x, const void* a, void* stream) {
+  FF_CHECK_ARG(x && a && na >= 1 && n % na == 0, "ff_real_mul: bad argument");
+  FF_PREC_DISPATCH(prec, LAUNCH1D(k_real_mul<double>, n, n, na, (double*)x, (const double*)a),
+                   LAUNCH1D(k_real_mul<float>, n, n, na, (float*)x, (const float*)a));
+  return FF_OK;
+}
+
+int ff_parsevalsum2(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft_form, double norm, double* out,
+                    void* stream) {
+  FF_CHECK_ARG(uh && out && n0 >= 1 && nrest >= 1, "ff_parsevalsum2: bad argument");
+  FF_PREC_DISPATCH(prec, return parseval<double>(uh, n0, nrest, rfft_form, 0, norm, out, (cudaStream_t)stream),
+                   return parseval<float>(uh, n0, nrest, rfft_form, 0, norm, out, (cudaStream_t)stream));
+  return FF_OK;
+}
+
+int ff_parsevalsum2_weighted(int prec, const void* uh, const void* wt, int64_t n0, int64_t nrest, int rfft_form,
+                             double norm, double* out, double* dev_out, void* stream) {
+  FF_CHECK_ARG(uh && (out || dev_out) && n0 >= 1 && nrest >= 1, "ff_parsevalsum2_weighted: bad argument");
+  FF_PREC_DISPATCH(prec,
+      return parseval<double>(uh, n0, nrest, rfft_form, 0, norm, out, (cudaStream_t)stream, wt, dev_out),
+      return parseval<float>(uh, n0, nrest, rfft_form, 0, norm, out, (cudaStream_t)stream, wt, dev_out));
+  return FF_OK;
+}
+
+int ff_vort_velocities(int prec, int64_t nkr, int64_t ny, const void* zh, const void* kr, const void* l,
+                       const void* invK, void* uh, void* vh, void* stream) {
+  FF_CHECK_ARG(zh && kr && l && invK && uh && vh && nkr >= 1 && ny >= 1, "ff_vort_velocities: bad argument");
+  const int64_t n = nkr * ny;
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_velocities<double>, n, nkr, n, (const double2*)zh, (const double*)kr, (const double*)l,
+               (const double*)invK, (double2*)uh, (double2*)vh),
+      LAUNCH1D(k_velocities<float>, n, nkr, n, (const float2*)zh, (const float*)kr, (const float*)l,
+               (const float*)invK, (float2*)uh, (float2*)vh));
+  return FF_OK;
+}
+
+int ff_parsevalsum(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft_form, double norm, double* out,
+                   void* stream) {
+  FF_CHECK_ARG(uh && out && n0 >= 1 && nrest >= 1, "ff_parsevalsum: bad argument");
+  FF_PREC_DISPATCH(prec, return parseval<double>(uh, n0, nrest, rfft_form, 1, norm, out, (cudaStream_t)stream),
+                   return parseval<float>(uh, n0, nrest, rfft_form, 1, norm, out, (cudaStream_t)stream));
+  return FF_OK;
+}
+
+}  // extern "C"

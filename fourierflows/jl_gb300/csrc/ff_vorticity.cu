@@ -1,0 +1,569 @@
+// Host side of the fused 2D vorticity path: problem descriptors, work lists, launch
+// geometry, CUDA-graph capture of whole steps and the tile/radix autotuner.
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ff_plan.cuh"
+#include "ff_vorticity.cuh"
+
+using namespace ff;
+
+namespace {
+
+struct Geom {
+  int tla = 0, tlc = 0, tlr = 0;   // tile widths of passes A, C and rows per CTA of pass B
+  int tha = 0, thb = 0, thc = 0;   // threads per CTA
+  size_t sma = 0, smb = 0, smc = 0;
+  int ga = 0, gb = 0, gc = 0;      // grid sizes
+  int radix_variant = 0;           // 0: radix-8 first, 1: radix-4 first, 2: small radix first
+};
+
+// factorisation variants explored by the autotuner
+bool factorize_variant(int n, int variant, LinePlan& P) {
+  if (!factorize(n, P)) return false;
+  if (variant == 1) {
+    // prefer radix 4: split each 8 into 4 * 2 pairs -> 8*8 = 4*4*4
+    int twos = 0, rest[FF_MAX_STAGES], nr = 0;
+    for (int s = 0; s < P.nst; ++s) {
+      int r = P.radix[s];
+      if (r == 8) twos += 3;
+      else if (r == 4) twos += 2;
+      else if (r == 2) twos += 1;
+      else rest[nr++] = r;
+    }
+    P.nst = 0;
+    while (twos >= 2) { P.radix[P.nst++] = 4; twos -= 2; }
+    if (twos) P.radix[P.nst++] = 2;
+    for (int i = 0; i < nr; ++i) P.radix[P.nst++] = rest[i];
+  } else if (variant == 2) {
+    std::reverse(P.radix, P.radix + P.nst);
+  }
+  return true;
+}
+
+int round32(int t, int lo, int hi) {
+  t = ((t + 31) / 32) * 32;
+  return std::max(lo, std::min(hi, t));
+}
+
+}  // namespace
+
+struct ff_vort {
+  int prec = FF_F64, stepper = FF_STEP_ETDRK4, dev = 0;
+  int64_t nprob = 0;
+  double dt = 0;
+  bool filtered = false;
+  std::vector<ff_vort_problem> host;  // as given
+  int max_nx = 0, max_ny = 0, max_nkd = 0;
+  // device allocations
+  void* d_probs = nullptr;     // VortProb<T>[nprob]
+  void* d_calc_prob = nullptr; // VortProb<T>[1] for ff_vort_calcN
+  void* d_work_a = nullptr;
+  void* d_work_b = nullptr;
+  void* d_work_c = nullptr;
+  void* d_calc_work = nullptr;  // single-problem work lists (a | b | c)
+  void* d_inputs = nullptr;     // const cx<T>*[5][nprob]: pass-A inputs per substep
+  void* d_calc_input = nullptr;
+  int nwork_a = 0, nwork_b = 0, nwork_c = 0;
+  std::vector<void*> tables;    // twiddle tables
+  void* d_W = nullptr;
+  void* d_Q = nullptr;
+  Geom g;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  bool use_graph = true;
+  std::vector<unsigned char> calc_host;  // staging for ff_vort_calcN descriptor + work
+  std::vector<unsigned char> host_desc;  // host copy of the device descriptors
+  size_t calc_cap = 0;
+};
+
+namespace {
+
+template <typename T> size_t elem() { return sizeof(cx<T>); }
+
+template <typename T> Geom choose_geom(const ff_vort* h, int tla, int tlc, int tlr, int variant) {
+  Geom g;
+  const int ny = h->max_ny, hx = h->max_nx / 2;
+  const size_t es = elem<T>();
+  g.tla = tla > 0 ? tla : (sizeof(T) == 8 ? 2 : 4);
+  g.tlc = tlc > 0 ? tlc : (sizeof(T) == 8 ? 1 : 2);
+  g.tlr = tlr > 0 ? tlr : (sizeof(T) == 8 ? 2 : 4);
+  while (g.tla > 1 && 2 * (size_t)g.tla * ny * es > 110 * 1024) g.tla /= 2;
+  while (g.tlc > 1 && 4 * (size_t)g.tlc * ny * es > 110 * 1024) g.tlc /= 2;
+  while (g.tlr > 1 && 4 * (size_t)g.tlr * rows_stride(hx, (int)es) * es > 110 * 1024) g.tlr /= 2;
+  g.sma = 2 * (size_t)g.tla * ny * es;
+  g.smc = 4 * (size_t)g.tlc * ny * es;
+  g.smb = 4 * (size_t)g.tlr * rows_stride(hx, (int)es) * es;
+  g.tha = round32(g.tla * ny / 8, 64, 512);
+  g.thc = round32(2 * g.tlc * ny / 8, 64, 512);
+  g.thb = round32(g.tlr * hx / 4, 64, 512);
+  g.radix_variant = variant;
+  return g;
+}
+
+template <typename T> int grid_for(const void* k, int threads, size_t smem, int nwork) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const int cap = per_sm * sm_count();
+  return std::max(1, std::min(nwork, cap));
+}
+
+template <typename T> int build(ff_vort* h, const Geom& geom) {
+  // descriptors, twiddles and work lists for the current geometry
+  for (void* p : h->tables) cudaFree(p);
+  h->tables.clear();
+  std::vector<VortProb<T>> probs(h->nprob);
+  std::vector<WorkItem> wa, wb, wc;
+  const size_t es = elem<T>();
+  int64_t woff = 0;
+  for (int64_t i = 0; i < h->nprob; ++i) {
+    const ff_vort_problem& q = h->host[i];
+    VortProb<T>& P = probs[i];
+    memset(&P, 0, sizeof(P));
+    P.nx = (int)q.nx;
+    P.ny = (int)q.ny;
+    P.nkr = (int)(q.nx / 2 + 1);
+    P.nkd = (int)q.nkd;
+    P.la = (int)q.la;
+    P.lb = (int)q.lb;
+    const double s = 1.0 / ((double)q.nx * (double)q.ny);
+    P.scale2 = (T)(s * s);
+    if (!factorize_variant(P.nx / 2, geom.radix_variant, P.Px) || !factorize_variant(P.ny, geom.radix_variant, P.Py)) {
+      set_error("ff_vort: grid %lld x %lld has a prime factor above %d", (long long)q.nx, (long long)q.ny,
+                FF_MAX_GENERIC_RADIX);
+      return FF_ERR_UNSUPPORTED;
+    }
+    std::vector<double> t;
+    void* d = nullptr;
+    host_twiddles(P.nx / 2, t);
+    if (int st = upload_table(t, sizeof(T) == 8 ? FF_F64 : FF_F32, &d)) return st;
+    h->tables.push_back(d);
+    P.twx = (const cx<T>*)d;
+    host_twiddles(P.ny, t);
+    if (int st = upload_table(t, sizeof(T) == 8 ? FF_F64 : FF_F32, &d)) return st;
+    h->tables.push_back(d);
+    P.twy = (const cx<T>*)d;
+    host_real_twiddles(P.nx, t);
+    if (int st = upload_table(t, sizeof(T) == 8 ? FF_F64 : FF_F32, &d)) return st;
+    h->tables.push_back(d);
+    P.rtw = (const cx<T>*)d;
+    P.kr = (const T*)q.kr;
+    P.l = (const T*)q.l;
+    P.invK = (const T*)q.invKrsq;
+    P.W = (cx<T>*)h->d_W + woff * 3;
+    P.Q = (cx<T>*)h->d_Q + woff * 2;
+    woff += (int64_t)P.nkd * P.ny;
+    P.sol = (cx<T>*)q.sol;
+    P.filter = (const T*)q.filter;
+    if (h->stepper == FF_STEP_ETDRK4) {
+      P.eL = (const T*)q.coef[0];
+      P.eh = (const T*)q.coef[1];
+      P.zc = (const T*)q.coef[2];
+      P.al = (const T*)q.coef[3];
+      P.be = (const T*)q.coef[4];
+      P.ga = (const T*)q.coef[5];
+    } else {
+      P.L = (const T*)q.coef[0];
+    }
+    if (h->stepper == FF_STEP_ETDRK4) {
+      P.s1 = (cx<T>*)q.buf[0];
+      P.s2 = (cx<T>*)q.buf[1];
+      P.n1 = (cx<T>*)q.buf[2];
+      P.n2 = (cx<T>*)q.buf[3];
+      P.n3 = (cx<T>*)q.buf[4];
+    } else if (h->stepper == FF_STEP_RK4) {
+      P.s1 = (cx<T>*)q.buf[0];
+      P.n1 = (cx<T>*)q.buf[1];
+      P.n2 = (cx<T>*)q.buf[2];
+      P.n3 = (cx<T>*)q.buf[3];
+    } else {
+      P.s1 = (cx<T>*)q.buf[0];
+    }
+    const int ta = (int)ceil_div(P.nkd, geom.tla);
+    for (int f = 0; f < 3; ++f)
+      for (int tt = 0; tt < ta; ++tt) wa.push_back({(int)i, tt, f, 0});
+    const int tb = (int)ceil_div(P.ny, geom.tlr);
+    for (int tt = 0; tt < tb; ++tt) wb.push_back({(int)i, tt, 0, 0});
+    const int tc = (int)ceil_div(P.nkr, geom.tlc);
+    for (int tt = 0; tt < tc; ++tt) wc.push_back({(int)i, tt, 0, 0});
+  }
+  // longest work first helps the persistent grid balance uneven sizes
+  auto by_size = [&](const WorkItem& a, const WorkItem& b) {
+    return (int64_t)probs[a.prob].nx * probs[a.prob].ny > (int64_t)probs[b.prob].nx * probs[b.prob].ny;
+  };
+  std::stable_sort(wa.begin(), wa.end(), by_size);
+  std::stable_sort(wb.begin(), wb.end(), by_size);
+  std::stable_sort(wc.begin(), wc.end(), by_size);
+  for (void** p : {&h->d_probs, &h->d_work_a, &h->d_work_b, &h->d_work_c, &h->d_inputs})
+    if (*p) { cudaFree(*p); *p = nullptr; }
+  h->host_desc.resize(sizeof(VortProb<T>) * h->nprob);
+  memcpy(h->host_desc.data(), probs.data(), h->host_desc.size());
+  FF_CUDA(cudaMalloc(&h->d_probs, sizeof(VortProb<T>) * h->nprob));
+  FF_CUDA(cudaMemcpy(h->d_probs, probs.data(), sizeof(VortProb<T>) * h->nprob, cudaMemcpyHostToDevice));
+  FF_CUDA(cudaMalloc(&h->d_work_a, sizeof(WorkItem) * wa.size()));
+  FF_CUDA(cudaMalloc(&h->d_work_b, sizeof(WorkItem) * wb.size()));
+  FF_CUDA(cudaMalloc(&h->d_work_c, sizeof(WorkItem) * wc.size()));
+  FF_CUDA(cudaMemcpy(h->d_work_a, wa.data(), sizeof(WorkItem) * wa.size(), cudaMemcpyHostToDevice));
+  FF_CUDA(cudaMemcpy(h->d_work_b, wb.data(), sizeof(WorkItem) * wb.size(), cudaMemcpyHostToDevice));
+  FF_CUDA(cudaMemcpy(h->d_work_c, wc.data(), sizeof(WorkItem) * wc.size(), cudaMemcpyHostToDevice));
+  h->nwork_a = (int)wa.size();
+  h->nwork_b = (int)wb.size();
+  h->nwork_c = (int)wc.size();
+  // pass-A input of each substep: sol, then the stepper's intermediate states
+  std::vector<const cx<T>*> in(5 * h->nprob);
+  for (int64_t i = 0; i < h->nprob; ++i) {
+    const VortProb<T>& P = probs[i];
+    const cx<T>* seq_etd[5] = {P.sol, P.s1, P.s2, P.s2, P.sol};
+    const cx<T>* seq_rk[5] = {P.sol, P.s1, P.s1, P.s1, P.sol};
+    for (int k = 0; k < 5; ++k) {
+      const cx<T>* p = P.sol;
+      if (h->stepper == FF_STEP_ETDRK4) p = seq_etd[k];
+      else if (h->stepper == FF_STEP_RK4) p = seq_rk[k];
+      in[k * h->nprob + i] = p;
+    }
+  }
+  FF_CUDA(cudaMalloc(&h->d_inputs, sizeof(void*) * in.size()));
+  FF_CUDA(cudaMemcpy(h->d_inputs, in.data(), sizeof(void*) * in.size(), cudaMemcpyHostToDevice));
+  h->g = geom;
+  if (int st = ensure_smem((const void*)k_vort_a<T>, geom.sma)) return st;
+  if (int st = ensure_smem((const void*)k_vort_b<T>, geom.smb)) return st;
+#define FF_SMEM_C(E) if (int st = ensure_smem((const void*)k_vort_c<T, E>, geom.smc)) return st;
+  FF_SMEM_C(EPI_N) FF_SMEM_C(EPI_ETD1) FF_SMEM_C(EPI_ETD2) FF_SMEM_C(EPI_ETD3) FF_SMEM_C(EPI_ETD4)
+  FF_SMEM_C(EPI_RK1) FF_SMEM_C(EPI_RK2) FF_SMEM_C(EPI_RK3) FF_SMEM_C(EPI_RK4) FF_SMEM_C(EPI_LS)
+#undef FF_SMEM_C
+  h->g.ga = grid_for<T>((const void*)k_vort_a<T>, geom.tha, geom.sma, h->nwork_a);
+  h->g.gb = grid_for<T>((const void*)k_vort_b<T>, geom.thb, geom.smb, h->nwork_b);
+  h->g.gc = grid_for<T>((const void*)k_vort_c<T, EPI_ETD1>, geom.thc, geom.smc, h->nwork_c);
+  if (h->exec) { cudaGraphExecDestroy(h->exec); h->exec = nullptr; }
+  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  return FF_OK;
+}
+
+template <typename T, int EPI>
+int launch_c(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, EpiScalars<T> S,
+             cudaStream_t s) {
+  k_vort_c<T, EPI><<<grid, h->g.thc, h->g.smc, s>>>((const VortProb<T>*)probs, (const WorkItem*)work, nwork,
+                                                     h->g.tlc, S);
+  FF_LAUNCHED("k_vort_c");
+  return FF_OK;
+}
+
+// one calcN! (passes A, B, C) with epilogue EPI on all problems; `inputs` = pass-A sources
+template <typename T, int EPI>
+int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s) {
+  const auto* P = (const VortProb<T>*)h->d_probs;
+  k_vort_a<T><<<h->g.ga, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)h->d_work_a, h->nwork_a, h->g.tla,
+                                                   (const cx<T>* const*)inputs);
+  FF_LAUNCHED("k_vort_a");
+  k_vort_b<T><<<h->g.gb, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)h->d_work_b, h->nwork_b, h->g.tlr);
+  FF_LAUNCHED("k_vort_b");
+  return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
+}
+
+template <typename T> int enqueue_step(const ff_vort* h, cudaStream_t s) {
+  const size_t stride = sizeof(void*) * h->nprob;
+  const char* in = (const char*)h->d_inputs;
+  const T dt = (T)h->dt;
+  EpiScalars<T> S{};
+  S.use_filter = h->filtered ? 1 : 0;
+  int st = FF_OK;
+  if (h->stepper == FF_STEP_ETDRK4) {
+    S.use_filter = 0;
+    if ((st = calc<T, EPI_ETD1>(h, in, S, s))) return st;
+    if ((st = calc<T, EPI_ETD2>(h, in + stride, S, s))) return st;
+    if ((st = calc<T, EPI_ETD3>(h, in + 2 * stride, S, s))) return st;
+    S.use_filter = h->filtered ? 1 : 0;
+    return calc<T, EPI_ETD4>(h, in + 3 * stride, S, s);
+  }
+  if (h->stepper == FF_STEP_RK4) {
+    const T half = (T)(dt / T(2));
+    S.use_filter = 0;
+    S.c = half;
+    if ((st = calc<T, EPI_RK1>(h, in, S, s))) return st;
+    if ((st = calc<T, EPI_RK2>(h, in + stride, S, s))) return st;
+    S.c = dt;
+    if ((st = calc<T, EPI_RK3>(h, in + 2 * stride, S, s))) return st;
+    S.c = (T)(dt / T(6));
+    S.use_filter = h->filtered ? 1 : 0;
+    return calc<T, EPI_RK4>(h, in + 3 * stride, S, s);
+  }
+  // LSRK54: Carpenter-Kennedy 2N-storage stages
+  for (int i = 0; i < 5; ++i) {
+    S.c = (T)h->host[0].lsrk_A[i];
+    S.b = (T)h->host[0].lsrk_B[i];
+    S.dt = dt;
+    S.first = i == 0;
+    S.use_filter = (i == 4 && h->filtered) ? 1 : 0;
+    if ((st = calc<T, EPI_LS>(h, in, S, s))) return st;
+  }
+  return FF_OK;
+}
+
+int enqueue(const ff_vort* h, cudaStream_t s) {
+  return h->prec == FF_F64 ? enqueue_step<double>(h, s) : enqueue_step<float>(h, s);
+}
+
+int capture(ff_vort* h) {
+  cudaStream_t cs;
+  FF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  int st = FF_OK;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) st = cuda_status(e, "ff_vort: begin capture");
+  if (st == FF_OK) {
+    st = enqueue(h, cs);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(cs, &g);
+    if (st == FF_OK && e != cudaSuccess) st = cuda_status(e, "ff_vort: end capture");
+    if (st == FF_OK) {
+      e = cudaGraphInstantiate(&h->exec, g, 0);
+      if (e != cudaSuccess) st = cuda_status(e, "ff_vort: graph instantiate");
+      h->graph = g;
+    } else if (g) {
+      cudaGraphDestroy(g);
+    }
+  }
+  cudaStreamDestroy(cs);
+  return st;
+}
+
+int rebuild(ff_vort* h, int tla, int tlc, int tlr, int variant) {
+  if (h->prec == FF_F64) return build<double>(h, choose_geom<double>(h, tla, tlc, tlr, variant));
+  return build<float>(h, choose_geom<float>(h, tla, tlc, tlr, variant));
+}
+
+void destroy(ff_vort* h) {
+  if (!h) return;
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  for (void* p : h->tables) cudaFree(p);
+  for (void* p : {h->d_probs, h->d_calc_prob, h->d_work_a, h->d_work_b, h->d_work_c, h->d_calc_work, h->d_inputs,
+                  h->d_calc_input, h->d_W, h->d_Q})
+    if (p) cudaFree(p);
+  delete h;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ff_vort_create(int prec, int stepper, int filtered, double dt, int64_t nprob, const ff_vort_problem* probs,
+                   ff_vort** out) {
+  FF_CHECK_ARG(out && probs && nprob >= 1, "ff_vort_create: bad arguments");
+  *out = nullptr;
+  FF_CHECK_ARG(prec == FF_F64 || prec == FF_F32, "ff_vort_create: bad precision %d", prec);
+  FF_CHECK_ARG(stepper == FF_STEP_ETDRK4 || stepper == FF_STEP_RK4 || stepper == FF_STEP_LSRK54,
+               "ff_vort_create: unsupported stepper %d", stepper);
+  const int64_t maxn = prec == FF_F64 ? 4096 : 8192;
+  for (int64_t i = 0; i < nprob; ++i) {
+    const ff_vort_problem& q = probs[i];
+    FF_CHECK_ARG(q.nx >= 2 && q.ny >= 2 && q.nx % 2 == 0 && q.ny % 2 == 0,
+                 "ff_vort_create: problem %lld: nx, ny must be even and >= 2", (long long)i);
+    FF_CHECK_ARG(q.nx / 2 <= maxn && q.ny <= maxn, "ff_vort_create: problem %lld: grid too large", (long long)i);
+    FF_CHECK_ARG(q.nkd >= 1 && q.nkd <= q.nx / 2 + 1, "ff_vort_create: problem %lld: bad nkd", (long long)i);
+    FF_CHECK_ARG(q.la >= 0 && q.la <= q.lb && q.lb <= q.ny, "ff_vort_create: problem %lld: bad l range",
+                 (long long)i);
+    FF_CHECK_ARG(q.kr && q.l && q.invKrsq && q.sol, "ff_vort_create: problem %lld: null array", (long long)i);
+    if (stepper == FF_STEP_ETDRK4) {
+      for (int k = 0; k < 5; ++k) FF_CHECK_ARG(q.buf[k], "ff_vort_create: ETDRK4 needs 5 buffers");
+      for (int k = 0; k < 6; ++k) FF_CHECK_ARG(q.coef[k], "ff_vort_create: ETDRK4 needs 6 coefficient arrays");
+    } else if (stepper == FF_STEP_RK4) {
+      for (int k = 0; k < 4; ++k) FF_CHECK_ARG(q.buf[k], "ff_vort_create: RK4 needs 4 buffers");
+      FF_CHECK_ARG(q.coef[0], "ff_vort_create: RK4 needs L");
+    } else {
+      FF_CHECK_ARG(q.buf[0] && q.coef[0], "ff_vort_create: LSRK54 needs S2 and L");
+    }
+    if (filtered) FF_CHECK_ARG(q.filter, "ff_vort_create: filtered stepper without a filter");
+  }
+  ff_vort* h = new ff_vort();
+  h->prec = prec;
+  h->stepper = stepper;
+  h->filtered = filtered != 0;
+  h->dt = dt;
+  h->nprob = nprob;
+  h->host.assign(probs, probs + nprob);
+  cudaGetDevice(&h->dev);
+  int64_t wsize = 0;
+  for (auto& q : h->host) {
+    h->max_nx = std::max<int>(h->max_nx, (int)q.nx);
+    h->max_ny = std::max<int>(h->max_ny, (int)q.ny);
+    h->max_nkd = std::max<int>(h->max_nkd, (int)q.nkd);
+    wsize += q.nkd * q.ny;
+  }
+  const size_t es = prec == FF_F64 ? 16 : 8;
+  int st = FF_OK;
+  cudaError_t e = cudaMalloc(&h->d_W, 3 * wsize * es);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_Q, 2 * wsize * es);
+  if (e != cudaSuccess) st = cuda_status(e, "ff_vort_create: workspace");
+  if (st == FF_OK) {
+    const char* nog = getenv("FF_NO_GRAPH");
+    h->use_graph = !(nog && nog[0] == '1');
+    st = rebuild(h, 0, 0, 0, 0);
+  }
+  if (st != FF_OK) {
+    destroy(h);
+    return st;
+  }
+  *out = h;
+  return FF_OK;
+}
+
+int ff_vort_destroy(ff_vort* h) {
+  destroy(h);
+  return FF_OK;
+}
+
+int ff_vort_step(ff_vort* h, int64_t nsteps, void* stream) {
+  FF_CHECK_ARG(h, "ff_vort_step: null handle");
+  FF_CHECK_ARG(nsteps >= 0, "ff_vort_step: negative step count");
+  auto s = (cudaStream_t)stream;
+  if (!h->use_graph) {
+    for (int64_t i = 0; i < nsteps; ++i)
+      if (int st = enqueue(h, s)) return st;
+    return FF_OK;
+  }
+  if (!h->exec)
+    if (int st = capture(h)) return st;
+  for (int64_t i = 0; i < nsteps; ++i) FF_CUDA(cudaGraphLaunch(h->exec, s));
+  return FF_OK;
+}
+
+int ff_vort_config(const ff_vort* h, int32_t cfg[8]) {
+  FF_CHECK_ARG(h && cfg, "ff_vort_config: null argument");
+  cfg[0] = h->g.tla;
+  cfg[1] = h->g.tlc;
+  cfg[2] = h->g.tlr;
+  cfg[3] = h->g.radix_variant;
+  cfg[4] = h->g.tha;
+  cfg[5] = h->g.thb;
+  cfg[6] = h->g.thc;
+  cfg[7] = h->use_graph ? 1 : 0;
+  return FF_OK;
+}
+
+int ff_vort_set_config(ff_vort* h, int tla, int tlc, int tlr, int radix_variant) {
+  FF_CHECK_ARG(h, "ff_vort_set_config: null handle");
+  FF_CHECK_ARG(radix_variant >= 0 && radix_variant <= 2, "ff_vort_set_config: radix variant 0..2");
+  FF_CUDA(cudaDeviceSynchronize());
+  return rebuild(h, tla, tlc, tlr, radix_variant);
+}
+
+int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best_ms) {
+  FF_CHECK_ARG(h, "ff_vort_autotune: null handle");
+  // The trial steps advance the state: callers pass a scratch copy or restore it.
+  auto s = (cudaStream_t)stream;
+  const int reps = steps_per_trial > 0 ? steps_per_trial : 3;
+  const int tls_f64[] = {1, 2, 4};
+  const int tls_f32[] = {1, 2, 4, 8};
+  const int* tls = h->prec == FF_F64 ? tls_f64 : tls_f32;
+  const int ntl = h->prec == FF_F64 ? 3 : 4;
+  double best = 1e30;
+  int bcfg[4] = {0, 0, 0, 0};
+  cudaEvent_t e0, e1;
+  FF_CUDA(cudaEventCreate(&e0));
+  FF_CUDA(cudaEventCreate(&e1));
+  int st = FF_OK;
+  for (int v = 0; v < 3 && st == FF_OK; ++v)
+    for (int ia = 0; ia < ntl && st == FF_OK; ++ia)
+      for (int ic = 0; ic < ntl && st == FF_OK; ++ic)
+        for (int ir = 0; ir < ntl && st == FF_OK; ++ir) {
+          FF_CUDA(cudaStreamSynchronize(s));
+          st = rebuild(h, tls[ia], tls[ic], tls[ir], v);
+          if (st) break;
+          // skip configurations the size limits clamped to an already tried one
+          if (h->g.tla != tls[ia] || h->g.tlc != tls[ic] || h->g.tlr != tls[ir]) continue;
+          if ((st = ff_vort_step(h, 1, s))) break;  // warm-up (and graph capture)
+          FF_CUDA(cudaEventRecord(e0, s));
+          if ((st = ff_vort_step(h, reps, s))) break;
+          FF_CUDA(cudaEventRecord(e1, s));
+          FF_CUDA(cudaEventSynchronize(e1));
+          float ms = 0;
+          FF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          const double per = ms / reps;
+          if (per < best) {
+            best = per;
+            bcfg[0] = tls[ia];
+            bcfg[1] = tls[ic];
+            bcfg[2] = tls[ir];
+            bcfg[3] = v;
+          }
+        }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  FF_CUDA(cudaStreamSynchronize(s));
+  if ((st = rebuild(h, bcfg[0], bcfg[1], bcfg[2], bcfg[3]))) return st;
+  if (best_ms) *best_ms = best;
+  return FF_OK;
+}
+
+int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream) {
+  FF_CHECK_ARG(h && sol && N, "ff_vort_calcN: null argument");
+  FF_CHECK_ARG(prob >= 0 && prob < h->nprob, "ff_vort_calcN: problem index out of range");
+  auto s = (cudaStream_t)stream;
+  // single-problem descriptor copy with sol -> input and n1 -> N, and its work lists
+  const bool f64 = h->prec == FF_F64;
+  const size_t psz = f64 ? sizeof(VortProb<double>) : sizeof(VortProb<float>);
+  std::vector<unsigned char> desc(h->host_desc.begin() + psz * prob, h->host_desc.begin() + psz * (prob + 1));
+  int nx, ny, nkd, nkr;
+  if (f64) {
+    auto* P = (VortProb<double>*)desc.data();
+    P->n1 = (double2*)N;
+    nx = P->nx; ny = P->ny; nkd = P->nkd; nkr = P->nkr;
+  } else {
+    auto* P = (VortProb<float>*)desc.data();
+    P->n1 = (float2*)N;
+    nx = P->nx; ny = P->ny; nkd = P->nkd; nkr = P->nkr;
+  }
+  (void)nx;
+  std::vector<WorkItem> wa, wb, wc;
+  for (int f = 0; f < 3; ++f)
+    for (int t = 0; t < (int)ceil_div(nkd, h->g.tla); ++t) wa.push_back({0, t, f, 0});
+  for (int t = 0; t < (int)ceil_div(ny, h->g.tlr); ++t) wb.push_back({0, t, 0, 0});
+  for (int t = 0; t < (int)ceil_div(nkr, h->g.tlc); ++t) wc.push_back({0, t, 0, 0});
+  const size_t nw = wa.size() + wb.size() + wc.size();
+  const size_t bytes = psz + nw * sizeof(WorkItem) + sizeof(void*);
+  // the staging buffer persists so that the asynchronous copies below can read it
+  h->calc_host.resize(bytes);
+  unsigned char* hp = h->calc_host.data();
+  memcpy(hp, desc.data(), psz);
+  memcpy(hp + psz, wa.data(), wa.size() * sizeof(WorkItem));
+  memcpy(hp + psz + wa.size() * sizeof(WorkItem), wb.data(), wb.size() * sizeof(WorkItem));
+  memcpy(hp + psz + (wa.size() + wb.size()) * sizeof(WorkItem), wc.data(), wc.size() * sizeof(WorkItem));
+  memcpy(hp + psz + nw * sizeof(WorkItem), &sol, sizeof(void*));
+  if (bytes > h->calc_cap) {
+    // grown at most a few times; the free waits for earlier calls that read it
+    if (h->d_calc_prob) cudaFree(h->d_calc_prob);
+    h->d_calc_prob = nullptr;
+    FF_CUDA(cudaMalloc(&h->d_calc_prob, bytes));
+    h->calc_cap = bytes;
+  }
+  // stream-ordered: kernels of an earlier call on this stream finish first; the host
+  // staging buffer may be reused as soon as the call returns (pageable copy)
+  FF_CUDA(cudaMemcpyAsync(h->d_calc_prob, hp, bytes, cudaMemcpyHostToDevice, s));
+  const char* base = (const char*)h->d_calc_prob;
+  const void* dwa = base + psz;
+  const void* dwb = base + psz + wa.size() * sizeof(WorkItem);
+  const void* dwc = base + psz + (wa.size() + wb.size()) * sizeof(WorkItem);
+  const void* din = base + psz + nw * sizeof(WorkItem);
+  if (f64) {
+    auto* P = (const VortProb<double>*)base;
+    k_vort_a<double><<<(int)wa.size(), h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)dwa, (int)wa.size(), h->g.tla,
+                                                                 (const double2* const*)din);
+    FF_LAUNCHED("k_vort_a");
+    k_vort_b<double><<<(int)wb.size(), h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)dwb, (int)wb.size(), h->g.tlr);
+    FF_LAUNCHED("k_vort_b");
+    return launch_c<double, EPI_N>(h, base, dwc, (int)wc.size(), (int)wc.size(), EpiScalars<double>{}, s);
+  }
+  auto* P = (const VortProb<float>*)base;
+  k_vort_a<float><<<(int)wa.size(), h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)dwa, (int)wa.size(), h->g.tla,
+                                                              (const float2* const*)din);
+  FF_LAUNCHED("k_vort_a");
+  k_vort_b<float><<<(int)wb.size(), h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)dwb, (int)wb.size(), h->g.tlr);
+  FF_LAUNCHED("k_vort_b");
+  return launch_c<float, EPI_N>(h, base, dwc, (int)wc.size(), (int)wc.size(), EpiScalars<float>{}, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,296 @@
+// Fused 2D vorticity nonlinear term and time-stepper substeps (device side).
+//
+// One evaluation of N = -J(psi, zeta) = -(d/dx (u zeta) + d/dy (v zeta)) on the rfft
+// half spectrum (nkr, ny) is three passes, each reading and writing HBM once:
+//
+//   A  column pass, per tile of kept kr columns and per field f in {u, v, zeta}:
+//      gather zeta_hat with the 2/3 mask, form u_hat = i l zeta_hat / K^2,
+//      v_hat = -i kr zeta_hat / K^2 or zeta_hat, inverse FFT along y  -> W[f]
+//   B  row pass, per y row: three C2R transforms along x (half-length packing), the
+//      products u zeta and v zeta in physical space, two R2C transforms  -> Q[0..1]
+//   C  column pass, per tile of kr columns: forward FFTs along y of Q[0..1],
+//      N_hat = -(i kr Q0 + i l Q1) with the output mask, then the stepper's substep
+//      combination (the "epilogue") on the same tile.
+//
+// Only the kept columns kr < nkd (nkd = first aliased column) are carried through
+// W and Q: the aliased modes of the input are zero after masking and those of the
+// output are zeroed, so they are never transformed.  Physical-space fields never
+// reach HBM.
+//
+// Every kernel walks a work list of (problem, tile) items over an array of problem
+// descriptors, so one launch serves a single grid or an ensemble of grids of
+// different sizes (grid-stride over the list: a persistent launch).
+#pragma once
+
+#include "ff_fft.cuh"
+
+namespace ff {
+
+enum Epilogue {
+  EPI_N = 0,      // n1 = N (the bare calcN!)
+  EPI_ETD1 = 1,   // n1 = N; s1 = eh sol + zc N
+  EPI_ETD2 = 2,   // n2 = N; s2 = eh sol + zc N
+  EPI_ETD3 = 3,   // n3 = N; s2 = eh s1 + zc (2N - n1)
+  EPI_ETD4 = 4,   // sol = [f](eL sol + al n1 + 2 be (n2 + n3) + ga N)
+  EPI_RK1 = 5,    // n1 = N + L sol; s1 = sol + c n1
+  EPI_RK2 = 6,    // n2 = N + L s1;  s1 = sol + c n2
+  EPI_RK3 = 7,    // n3 = N + L s1;  s1 = sol + c n3
+  EPI_RK4 = 8,    // sol = [f](sol + c (n1 + 2 n2 + 2 n3 + (N + L s1)))
+  EPI_LS = 9,     // r = N + L sol; s1 = (first ? dt r : A s1 + dt r); sol = [f](sol + B s1)
+};
+
+template <typename T> struct VortProb {
+  int nx, ny, nkr, nkd;  // nkd: kept kr columns [0, nkd)
+  int la, lb;            // aliased l rows [la, lb)
+  T scale2;              // 1 / (nx ny)^2, applied to each physical product
+  LinePlan Px, Py;       // length nx/2 and ny
+  const cx<T>* twx;
+  const cx<T>* twy;
+  const cx<T>* rtw;      // packing twiddles, nx/2 + 1
+  const T* kr;           // nkr
+  const T* l;            // ny
+  const T* invK;         // nkr * ny, 1/K^2 with the mean mode 0
+  cx<T>* W;              // 3 * nkd * ny
+  cx<T>* Q;              // 2 * nkd * ny
+  // stepper state (nkr * ny each)
+  cx<T>* sol;
+  cx<T>* s1;
+  cx<T>* s2;
+  cx<T>* n1;
+  cx<T>* n2;
+  cx<T>* n3;
+  const T* L;   // linear operator (RK4 / LSRK54)
+  const T* eL;  // ETDRK4: exp(L dt), exp(L dt / 2), zeta, alpha, beta, Gamma
+  const T* eh;
+  const T* zc;
+  const T* al;
+  const T* be;
+  const T* ga;
+  const T* filter;
+};
+
+struct WorkItem {
+  int prob, tile, field, pad;
+};
+
+// per-launch scalars of the epilogue
+template <typename T> struct EpiScalars {
+  T c;      // dt/2, dt, dt/6 (RK); A (LS)
+  T b;      // B (LS)
+  T dt;     // dt (LS)
+  int first;
+  int use_filter;
+};
+
+// ---------------------------------------------------------------------------------------
+// pass A
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_vort_a(const VortProb<T>* __restrict__ probs,
+                                                const WorkItem* __restrict__ work, int nwork, int tl,
+                                                const cx<T>* const* __restrict__ inputs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    const cx<T>* zh = inputs[it.prob];
+    const int ny = P.ny, nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb, f = it.field;
+    const AddrTile ad{tl};
+    cx<T>* A = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* B = A + tl * ny;
+    const int c0 = it.tile * tl;
+    for (int idx = threadIdx.x; idx < tl * ny; idx += blockDim.x) {
+      const int ln = idx % tl, j = idx / tl, c = c0 + ln;
+      cx<T> v = czero<T>();
+      if (c < nkd && (j < la || j >= lb)) {
+        const int64_t e = (int64_t)c + (int64_t)j * nkr;
+        const cx<T> z = zh[e];
+        if (f == 0) v = mul_i(scl(z, P.l[j] * P.invK[e]));
+        else if (f == 1) v = mul_mi(scl(z, P.kr[c] * P.invK[e]));
+        else v = z;
+      }
+      A[ad(ln, j)] = v;
+    }
+    __syncthreads();
+    const cx<T>* R = fft_lines<T, 1>(A, B, P.twy, P.Py, tl, ad);
+    cx<T>* Wf = P.W + (int64_t)f * nkd * ny;
+    for (int idx = threadIdx.x; idx < tl * ny; idx += blockDim.x) {
+      const int ln = idx % tl, j = idx / tl, c = c0 + ln;
+      if (c < nkd) Wf[c + (int64_t)j * nkd] = R[ad(ln, j)];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// pass B
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_vort_b(const VortProb<T>* __restrict__ probs,
+                                                const WorkItem* __restrict__ work, int nwork, int tlr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    const int nx = P.nx, ny = P.ny, nkd = P.nkd, h = nx / 2;
+    const AddrRows ad{rows_stride(h, sizeof(cx<T>)), rows_pad_shift(sizeof(cx<T>))};
+    const int bufsz = tlr * ad.stride;
+    cx<T>* b0 = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* b[4] = {b0, b0 + bufsz, b0 + 2 * bufsz, b0 + 3 * bufsz};
+    const int row0 = it.tile * tlr;
+    const int64_t fstride = (int64_t)nkd * ny;
+    // gather the three y-transformed fields and pack them for the C2R transforms
+    for (int idx = threadIdx.x; idx < 3 * tlr * h; idx += blockDim.x) {
+      const int f = idx / (tlr * h);
+      const int r = idx - f * tlr * h;
+      const int ln = r / h, k = r - ln * h;
+      const int j = row0 + ln;
+      cx<T> v = czero<T>();
+      if (j < ny) {
+        const cx<T>* src = P.W + f * fstride + (int64_t)j * nkd;
+        const cx<T> xk = k < nkd ? src[k] : czero<T>();
+        const cx<T> xh = (h - k) < nkd ? src[h - k] : czero<T>();
+        v = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]));
+      }
+      b[f][ad(ln, k)] = v;
+    }
+    __syncthreads();
+    cx<T>* spare = b[3];
+    cx<T>* r[3];
+    for (int f = 0; f < 3; ++f) {
+      r[f] = fft_lines<T, 1>(b[f], spare, P.twx, P.Px, tlr, ad);
+      if (r[f] == spare) spare = b[f];
+    }
+    // products in physical space (packed real pairs), normalisation folded in
+    const T s2 = P.scale2;
+    for (int idx = threadIdx.x; idx < tlr * h; idx += blockDim.x) {
+      const int ln = idx / h, m = idx - ln * h;
+      const int a = ad(ln, m);
+      const cx<T> u = r[0][a], v = r[1][a], z = r[2][a];
+      r[0][a] = mk<T>(u.x * z.x * s2, u.y * z.y * s2);
+      r[1][a] = mk<T>(v.x * z.x * s2, v.y * z.y * s2);
+    }
+    __syncthreads();
+    const cx<T>* q0 = fft_lines<T, -1>(r[0], spare, P.twx, P.Px, tlr, ad);
+    const cx<T>* q1 = fft_lines<T, -1>(r[1], r[2], P.twx, P.Px, tlr, ad);
+    // unpack the kept columns of the two real transforms
+    for (int idx = threadIdx.x; idx < tlr * nkd; idx += blockDim.x) {
+      const int ln = idx / nkd, k = idx - ln * nkd;
+      const int j = row0 + ln;
+      if (j >= ny) continue;
+      cx<T> x0, x1;
+      if (k == 0 || k == h) {
+        const cx<T> z0 = q0[ad(ln, 0)], z1 = q1[ad(ln, 0)];
+        x0 = k == 0 ? mk<T>(z0.x + z0.y, T(0)) : mk<T>(z0.x - z0.y, T(0));
+        x1 = k == 0 ? mk<T>(z1.x + z1.y, T(0)) : mk<T>(z1.x - z1.y, T(0));
+      } else {
+        const cx<T> w = __ldg(&P.rtw[k]);
+        cx<T> dummy;
+        r2c_pair<T>(q0[ad(ln, k)], q0[ad(ln, h - k)], w, x0, dummy);
+        r2c_pair<T>(q1[ad(ln, k)], q1[ad(ln, h - k)], w, x1, dummy);
+      }
+      P.Q[(int64_t)j * nkd + k] = x0;
+      P.Q[fstride + (int64_t)j * nkd + k] = x1;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// pass C
+// ---------------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ cx<T> rmul(const T* c, int64_t e, cx<T> v) { return scl(v, c[e]); }
+
+template <typename T, int EPI>
+__device__ __forceinline__ void epilogue(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e, cx<T> N) {
+  if (EPI == EPI_N) {
+    P.n1[e] = N;
+  } else if (EPI == EPI_ETD1) {
+    P.n1[e] = N;
+    P.s1[e] = add(rmul(P.eh, e, P.sol[e]), rmul(P.zc, e, N));
+  } else if (EPI == EPI_ETD2) {
+    P.n2[e] = N;
+    P.s2[e] = add(rmul(P.eh, e, P.sol[e]), rmul(P.zc, e, N));
+  } else if (EPI == EPI_ETD3) {
+    P.n3[e] = N;
+    P.s2[e] = add(rmul(P.eh, e, P.s1[e]), rmul(P.zc, e, sub(scl(N, T(2)), P.n1[e])));
+  } else if (EPI == EPI_ETD4) {
+    cx<T> v = add(rmul(P.eL, e, P.sol[e]), rmul(P.al, e, P.n1[e]));
+    v = add(v, scl(rmul(P.be, e, add(P.n2[e], P.n3[e])), T(2)));
+    v = add(v, rmul(P.ga, e, N));
+    if (S.use_filter) v = scl(v, P.filter[e]);
+    P.sol[e] = v;
+  } else if (EPI == EPI_RK1) {
+    const cx<T> s = P.sol[e];
+    const cx<T> r = add(N, rmul(P.L, e, s));
+    P.n1[e] = r;
+    P.s1[e] = add(s, scl(r, S.c));
+  } else if (EPI == EPI_RK2 || EPI == EPI_RK3) {
+    const cx<T> r = add(N, rmul(P.L, e, P.s1[e]));
+    if (EPI == EPI_RK2) P.n2[e] = r;
+    else P.n3[e] = r;
+    P.s1[e] = add(P.sol[e], scl(r, S.c));
+  } else if (EPI == EPI_RK4) {
+    const cx<T> r4 = add(N, rmul(P.L, e, P.s1[e]));
+    const cx<T> acc = add(add(add(P.n1[e], scl(P.n2[e], T(2))), scl(P.n3[e], T(2))), r4);
+    cx<T> v = add(P.sol[e], scl(acc, S.c));
+    if (S.use_filter) v = scl(v, P.filter[e]);
+    P.sol[e] = v;
+  } else if (EPI == EPI_LS) {
+    const cx<T> s = P.sol[e];
+    const cx<T> r = add(N, rmul(P.L, e, s));
+    const cx<T> q = S.first ? scl(r, S.dt) : add(scl(P.s1[e], S.c), scl(r, S.dt));
+    P.s1[e] = q;
+    cx<T> v = add(s, scl(q, S.b));
+    if (S.use_filter) v = scl(v, P.filter[e]);
+    P.sol[e] = v;
+  }
+}
+
+template <typename T, int EPI>
+__global__ void __launch_bounds__(512) k_vort_c(const VortProb<T>* __restrict__ probs,
+                                                const WorkItem* __restrict__ work, int nwork, int tl,
+                                                EpiScalars<T> S) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    const int ny = P.ny, nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb;
+    const int c0 = it.tile * tl;
+    if (c0 < nkd) {
+      // two fields as 2*tl interleaved lines: line ln = field * tl + column
+      const int nl = 2 * tl;
+      const AddrTile ad{nl};
+      cx<T>* A = reinterpret_cast<cx<T>*>(smem_raw);
+      cx<T>* B = A + nl * ny;
+      const int64_t fstride = (int64_t)nkd * ny;
+      for (int idx = threadIdx.x; idx < nl * ny; idx += blockDim.x) {
+        const int ln = idx % nl, j = idx / nl;
+        const int f = ln / tl, c = c0 + (ln - f * tl);
+        A[ad(ln, j)] = c < nkd ? P.Q[f * fstride + c + (int64_t)j * nkd] : czero<T>();
+      }
+      __syncthreads();
+      const cx<T>* R = fft_lines<T, -1>(A, B, P.twy, P.Py, nl, ad);
+      for (int idx = threadIdx.x; idx < tl * ny; idx += blockDim.x) {
+        const int ln = idx % tl, j = idx / tl, c = c0 + ln;
+        if (c >= nkr) continue;
+        cx<T> N = czero<T>();
+        if (c < nkd && (j < la || j >= lb)) {
+          const cx<T> qa = R[ad(ln, j)], qb = R[ad(ln + tl, j)];
+          // N = -(i kr qa + i l qb)
+          N = mul_mi(add(scl(qa, P.kr[c]), scl(qb, P.l[j])));
+        }
+        epilogue<T, EPI>(P, S, (int64_t)c + (int64_t)j * nkr, N);
+      }
+      __syncthreads();
+    } else {
+      // aliased columns: N = 0, only the linear part of the substep
+      for (int idx = threadIdx.x; idx < tl * ny; idx += blockDim.x) {
+        const int ln = idx % tl, j = idx / tl, c = c0 + ln;
+        if (c < nkr) epilogue<T, EPI>(P, S, (int64_t)c + (int64_t)j * nkr, czero<T>());
+      }
+    }
+  }
+}
+
+}  // namespace ff

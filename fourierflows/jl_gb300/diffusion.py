@@ -1,0 +1,127 @@
+"""The Diffusion module (src/diffusion.jl:1-178) on libfourierflows_gb300.
+
+``Problem(dev; nx, Lx, kappa, dt, stepper, aliased_fraction, T)`` builds the 1D diffusion
+problem of the reference: constant kappa gives L = -kappa kr^2 and N = 0; an array kappa
+gives L = 0 and N = d/dx(kappa dc/dx) computed with two transforms.  ``Problem3D`` is
+the ThreeDGrid constant-kappa variant (L = -kappa Krsq) used by the ensemble form.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib
+from .devices import GPU, cxtype, device_array, on_device, prec_of, ptr, stream_handle, zeros
+from .domains import OneDGrid, ThreeDGrid
+from .plans import ldiv_, mul_
+from .problem import AbstractParams, AbstractVars, Equation as _Equation, Problem as _Problem
+from .utils import _mul_ik
+
+
+class Params(AbstractParams):
+    """Params(kappa): diffusivity, a number or an array on the grid (src/diffusion.jl:68-74)."""
+
+    def __init__(self, kappa):
+        self.κ = kappa
+
+    @property
+    def kappa(self):
+        return self.κ
+
+
+def make_params(grid, kappa):
+    if np.ndim(kappa) == 0 and not on_device(kappa):
+        return Params(kappa)
+    return Params(device_array(grid.device)(np.asarray(kappa.cpu() if on_device(kappa) else kappa, dtype=grid.T)))
+
+
+class Vars(AbstractVars):
+    """c, cx (physical) and ch, cxh (spectral) (src/diffusion.jl:99-122)."""
+
+    def __init__(self, grid):
+        T = grid.T
+        dev = grid.device
+        self.c = zeros(dev, T, (grid.nx,))
+        self.cx = zeros(dev, T, (grid.nx,))
+        self.ch = zeros(dev, cxtype(T), (grid.nkr,))
+        self.cxh = zeros(dev, cxtype(T), (grid.nkr,))
+
+
+class _DiffusionCalcN:
+    """calcN!(N, sol, t, clock, vars, params, grid), src/diffusion.jl:129-143.
+
+    Constant kappa: N = 0.  Array kappa: cxh = i kr sol; cx = irfft(cxh); cx *= kappa;
+    cxh = rfft(cx); N = i kr cxh -- four native launches."""
+    __name__ = "calcN!"
+
+    def __call__(self, N, sol, t, clock, vars, params, grid):
+        k = params.κ
+        if not on_device(k):
+            N.zero_()  # @. N = 0 on a device buffer
+            return None
+        _mul_ik(vars.cxh, sol, grid.kr)
+        ldiv_(vars.cx, grid.rfftplan, vars.cxh)
+        _lib.call("ff_real_mul", prec_of(vars.cx.dtype), vars.cx.numel(), k.numel(), ptr(vars.cx, "cx"),
+                  ptr(k, "kappa"), stream_handle())
+        mul_(vars.cxh, grid.rfftplan, vars.cx)
+        _mul_ik(N, vars.cxh, grid.kr)
+        return None
+
+
+calcN_ = _DiffusionCalcN()
+
+
+def Equation(grid, params):
+    """L = -kappa kr^2 for constant kappa, else L = 0 with dims (nkr,) (src/diffusion.jl:82-90)."""
+    if on_device(params.κ):
+        return _Equation(0, calcN_, grid, dims=(grid.nkr,), T=cxtype(grid.T))
+    kr = grid.kr_host.reshape(-1).astype(np.float64)
+    L = (-params.κ * kr ** 2).astype(grid.T)
+    return _Equation(device_array(grid.device)(L), calcN_, grid)
+
+
+def Problem(dev=None, *, nx=128, Lx=2 * math.pi, κ=0, kappa=None, dt=0.01, stepper="RK4", aliased_fraction=0,
+            T=np.float64):
+    """Diffusion.Problem(dev; nx=128, Lx=2pi, kappa=0, dt=0.01, stepper="RK4",
+    aliased_fraction=0, T=Float64), src/diffusion.jl:44-59."""
+    dev = dev if dev is not None else GPU()
+    kappa = κ if kappa is None else kappa
+    grid = OneDGrid(dev, nx=nx, Lx=Lx, aliased_fraction=aliased_fraction, T=T)
+    params = make_params(grid, kappa)
+    vars = Vars(grid)
+    eq = Equation(grid, params)
+    return _Problem(eq, stepper, dt, grid, vars, params)
+
+
+def updatevars_(prob_or_vars, grid=None, sol=None):
+    """updatevars!(vars, grid, sol) / updatevars!(prob) (src/diffusion.jl:150-162)."""
+    if grid is None:
+        prob = prob_or_vars
+        vars, grid, sol = prob.vars, prob.grid, prob.sol
+    else:
+        vars = prob_or_vars
+    vars.ch.copy_(sol)
+    _mul_ik(vars.cxh, sol, grid.kr)
+    ldiv_(vars.c, grid.rfftplan, vars.ch)  # the native inverse never clobbers its input
+    ldiv_(vars.cx, grid.rfftplan, vars.cxh)
+    return None
+
+
+def set_c_(prob, c):
+    """set_c!(prob, c): sol = rfft(c), then updatevars! (src/diffusion.jl:167-176)."""
+    src = c if on_device(c) else device_array(prob.grid.device)(np.asarray(c, dtype=prob.grid.T))
+    prob.vars.c.copy_(src.reshape(prob.vars.c.shape))
+    mul_(prob.sol, prob.grid.rfftplan, prob.vars.c)
+    updatevars_(prob)
+    return None
+
+
+def Problem3D(dev=None, *, n, L=2 * math.pi, kappa, dt, stepper="ETDRK4", T=np.float64):
+    """Constant-kappa diffusion on a ThreeDGrid n^3: L = -kappa Krsq, N = 0."""
+    dev = dev if dev is not None else GPU()
+    grid = ThreeDGrid(dev, nx=n, Lx=L, aliased_fraction=0, T=T)
+    params = Params(kappa)
+    Lop = (-kappa * grid.Krsq_host.astype(np.float64)).astype(T)
+    eq = _Equation(device_array(dev)(Lop), calcN_, grid)
+    return _Problem(eq, stepper, dt, grid, None, params)

@@ -1,0 +1,229 @@
+/*
+ * libfourierflows_gb300 -- C ABI of the GB300 (sm_103a) pseudospectral time-stepping path.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream handle
+ * (cudaStream_t passed as void*, NULL = legacy default stream) and returns an int status
+ * (FF_OK = 0).  On failure ff_last_error() returns a message for the calling thread.
+ * Nothing here synchronises the stream unless it returns a host scalar (the Parseval
+ * reductions), mirroring the reference, whose GPU reductions return host numbers.
+ *
+ * Layout is the reference's (Julia, column-major): the first index is fastest.  A 2D
+ * real field is (nx, ny), its real transform (nkr, ny) with nkr = nx/2 + 1; complex
+ * numbers are interleaved (re, im) doubles (FF_F64) or floats (FF_F32).  Arrays beyond
+ * the grid's dimensions (fields, ensemble members) are trailing "batch" dimensions.
+ *
+ * Citations are FourierFlows.jl source lines (path:line) of the interface each entry
+ * point replaces.
+ */
+#ifndef FOURIERFLOWS_GB300_H
+#define FOURIERFLOWS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define FF_OK 0
+#define FF_ERR_ARG 1         /* bad argument (shape, size, pointer, alignment)           */
+#define FF_ERR_CUDA 2        /* a CUDA runtime call failed                                */
+#define FF_ERR_UNSUPPORTED 3 /* valid request this build does not implement (e.g. radix) */
+#define FF_ERR_ALLOC 4       /* device allocation failed                                 */
+#define FF_ERR_TIMEOUT 5     /* a bounded device-side wait gave up                       */
+
+/* ---- precisions ---------------------------------------------------------------------- */
+#define FF_F64 0
+#define FF_F32 1
+
+/* ---- coefficient descriptors --------------------------------------------------------- */
+/* A per-mode coefficient such as the linear operator L of Equation(L, calcN!, grid)
+ * (src/problem.jl:11-34): absent, a real or complex device array with one entry per
+ * state element, or a scalar (Diffusion with varying kappa uses L = 0,
+ * src/diffusion.jl:89-90).  Arrays are in the state's precision unless stated. */
+#define FF_COEF_NONE 0
+#define FF_COEF_REAL 1
+#define FF_COEF_COMPLEX 2
+#define FF_COEF_SCALAR 3 /* re (+ i im) */
+
+typedef struct {
+  const void* ptr;
+  int32_t kind;
+  int32_t pad_;
+  double re;
+  double im;
+} ff_coef;
+
+/* ---- library ------------------------------------------------------------------------- */
+int ff_version(void);                       /* (major << 16) | (minor << 8) | patch        */
+int ff_last_error(char* buf, size_t len);   /* copies the calling thread's last message   */
+
+/* ---- FFT plans ----------------------------------------------------------------------- */
+typedef struct ff_plan ff_plan;
+
+/* Real-to-complex plan over all ndim (1..3) dimensions n[0..ndim-1], applied to `batch`
+ * consecutive arrays.  Replaces plan_flows_rfft (src/domains.jl:3,5) as built by the
+ * grid constructors (src/domains.jl:87,208,349).  Every n must be even in dimension 0
+ * (odd sizes are rejected by the grids, src/domains.jl:66,179,316) and factor into
+ * primes <= 31 in every dimension, with n[d] <= 4096 (FF_F64) or 8192 (FF_F32). */
+int ff_plan_create(int ndim, const int64_t n[3], int prec, int64_t batch, ff_plan** plan);
+
+/* Complex-to-complex plan; replaces plan_flows_fft (src/domains.jl:2,4,86,207,348). */
+int ff_cplan_create(int ndim, const int64_t n[3], int prec, int64_t batch, ff_plan** plan);
+
+int ff_plan_destroy(ff_plan* plan);
+
+/* mul!(out, rfftplan, in): unnormalised forward transform, exp(-i k x) (src/diffusion.jl:139,171). */
+int ff_rfft(const ff_plan* plan, const void* in_real, void* out_complex, void* stream);
+
+/* ldiv!(out, rfftplan, in): inverse normalised by 1/(nx ny nz) (src/diffusion.jl:137,154-155).
+ * Unlike FFTW's c2r it never modifies its input. */
+int ff_irfft(const ff_plan* plan, const void* in_complex, void* out_real, void* stream);
+
+/* mul!/ldiv! with the complex plan; in == out is allowed. */
+int ff_fft(const ff_plan* plan, const void* in, void* out, void* stream);
+int ff_ifft(const ff_plan* plan, const void* in, void* out, void* stream);
+
+/* ---- dealias! (src/domains.jl:428-476) ------------------------------------------------ */
+/* Zero the index ranges [lo[d], hi[d]) (0-based, lo >= hi = empty) along dimension d of
+ * the array fh of complex size dims[0] x dims[1] x dims[2] x dims[3] (dims[3] = batch). */
+int ff_dealias(int prec, void* fh, const int64_t dims[4], const int64_t lo[3], const int64_t hi[3],
+               void* stream);
+
+/* ---- fused time-stepper substeps (src/timesteppers.jl) --------------------------------- */
+/* All act elementwise on n complex values; `filter` is a real array (state precision) or
+ * NULL; each is one pass over HBM.                                                       */
+
+/* ForwardEuler / FilteredForwardEuler update (src/timesteppers.jl:113,144):
+ *   sol = [filter *] (sol + dt (L sol + N)) */
+int ff_euler_update(int prec, int64_t n, void* sol, const void* N, ff_coef L, double dt, const void* filter,
+                    void* stream);
+
+/* RK4 addlinearterm! + substepsol! (src/timesteppers.jl:225-235,239-255):
+ *   RHS += L x;   if newsol: newsol = sol + c RHS          (x may alias newsol) */
+int ff_rk4_substep(int prec, int64_t n, void* RHS, ff_coef L, const void* x, const void* sol, void* newsol,
+                   double c, void* stream);
+
+/* last RK4 substep + RK4update! (+ filter) (src/timesteppers.jl:255,260-262,279):
+ *   RHS4 += L x;  sol = [filter *] (sol + c6 (RHS1 + 2 RHS2 + 2 RHS3 + RHS4)),
+ * c6 = dt/6 rounded to the state precision as the reference computes it. */
+int ff_rk4_update(int prec, int64_t n, void* sol, void* RHS4, ff_coef L, const void* x, const void* RHS1,
+                  const void* RHS2, const void* RHS3, double c6, const void* filter, void* stream);
+
+/* one LSRK54 stage (src/timesteppers.jl:383-395, + filter :408 when filter != NULL):
+ *   RHS += L sol;  S2 = A S2 + dt RHS (S2 = dt RHS if first);  sol = [filter *](sol + B S2) */
+int ff_lsrk54_stage(int prec, int64_t n, void* sol, void* RHS, void* S2, ff_coef L, double A, double B,
+                    double dt, int first, const void* filter, void* stream);
+
+/* ETDRK4substep12! (src/timesteppers.jl:506-510): out = e_half sol + zeta N */
+int ff_etdrk4_substep12(int prec, int64_t n, void* out, ff_coef e_half, const void* sol, ff_coef zeta,
+                        const void* N, void* stream);
+
+/* ETDRK4substep3! (src/timesteppers.jl:512-516): out = e_half sol1 + zeta (2 N3 - N1) */
+int ff_etdrk4_substep3(int prec, int64_t n, void* out, ff_coef e_half, const void* sol1, ff_coef zeta,
+                       const void* N1, const void* N3, void* stream);
+
+/* ETDRK4update! (+ filter) (src/timesteppers.jl:501-504,552):
+ *   sol = [filter *] (expL sol + alpha N1 + 2 beta (N2 + N3) + Gamma N4) */
+int ff_etdrk4_update(int prec, int64_t n, void* sol, ff_coef expL, ff_coef alpha, ff_coef beta, ff_coef Gamma,
+                     const void* N1, const void* N2, const void* N3, const void* N4, const void* filter,
+                     void* stream);
+
+/* AB3 step (src/timesteppers.jl:628-651,658): RHS += L sol; sol += dt RHS (euler != 0) or
+ * dt (23/12 RHS - 16/12 RHSm1 + 5/12 RHSm2); [sol *= filter]; RHSm2 = RHSm1; RHSm1 = RHS */
+int ff_ab3_update(int prec, int64_t n, void* sol, void* RHS, void* RHSm1, void* RHSm2, ff_coef L, double dt,
+                  int euler, const void* filter, void* stream);
+
+/* sol .*= filter (src/timesteppers.jl:279,408,552,658) */
+int ff_filter_mul(int prec, int64_t n, void* sol, const void* filter, void* stream);
+
+/* ---- spectral helpers ------------------------------------------------------------------ */
+/* out = i k in, k broadcast along dimension 0 (k has n0 entries), the pattern of
+ * `@. cxh = im * kr * sol` (src/diffusion.jl:136,140,154).  out may alias in. */
+int ff_mul_ik(int prec, int64_t n0, int64_t nrest, void* out, const void* in, const void* k, void* stream);
+
+/* x .*= a for real arrays of n elements, a real array of n or of n0 (broadcast along
+ * the trailing dimensions) -- `@. cx *= kappa` (src/diffusion.jl:138). */
+int ff_real_mul(int prec, int64_t n, int64_t na, void* x, const void* a, void* stream);
+
+/* parsevalsum2 / parsevalsum (src/utils.jl:113-183).  uh has n0 x nrest complex values;
+ * rfft_form != 0 counts rows 1..n0-2 twice (conjugate-symmetric half spectrum).  The
+ * result times `norm` is written to *out (host memory); the stream is synchronised. */
+int ff_parsevalsum2(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft_form, double norm,
+                    double* out, void* stream);
+int ff_parsevalsum(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft_form, double norm,
+                   double* out, void* stream);
+
+/* parsevalsum2 of uh .* sqrt(wt) for a real weight array wt (NULL = 1), e.g. the energy
+ * 1/2 parsevalsum2(zeta_hat sqrt(invKrsq)) / (Lx Ly) with wt = invKrsq.  With dev_out
+ * non-NULL the result goes to that device double and nothing synchronises (the
+ * diagnostic can be recorded inside a captured step); otherwise *out as above. */
+int ff_parsevalsum2_weighted(int prec, const void* uh, const void* wt, int64_t n0, int64_t nrest, int rfft_form,
+                             double norm, double* out, double* dev_out, void* stream);
+
+/* u_hat = -i l psi_hat, v_hat = i kr psi_hat with psi_hat = -zeta_hat invKrsq on the
+ * (nkr, ny) half spectrum: the velocity spectra of a vorticity field. */
+int ff_vort_velocities(int prec, int64_t nkr, int64_t ny, const void* zh, const void* kr, const void* l,
+                       const void* invKrsq, void* uh, void* vh, void* stream);
+
+/* ---- fused 2D vorticity steppers ------------------------------------------------------- */
+/* The nonlinear term N = -J(psi, zeta), psi_hat = -zeta_hat / |k|^2, of the 2D vorticity
+ * equation, with 2/3 dealiasing of its input and output, fused with the substeps of a
+ * time stepper.  The reference's call stack it replaces is stepforward!(prob) ->
+ * ETDRK4substeps! / RK4substeps! / LSRK54update! (src/timesteppers.jl:518-547,237-274,
+ * 383-404) -> the user calcN! built on jacobianh (src/utils.jl:190-205), rfftplan
+ * mul!/ldiv! and dealias! (src/domains.jl:428-476).  One handle advances one problem or
+ * an ensemble of problems of different sizes; every substep is three persistent
+ * launches over all problems, and a step is replayed from a captured CUDA graph. */
+typedef struct ff_vort ff_vort;
+
+#define FF_STEP_ETDRK4 0
+#define FF_STEP_RK4 1
+#define FF_STEP_LSRK54 2
+
+typedef struct {
+  int64_t nx, ny;       /* physical grid; nkr = nx/2 + 1                                    */
+  int64_t nkd;          /* kept kr columns [0, nkd): the first of kralias, or nkr if none   */
+  int64_t la, lb;       /* aliased l rows [la, lb) (0-based lalias); la == lb: none         */
+  const void* kr;       /* nkr wavenumbers (state precision)                                 */
+  const void* l;        /* ny wavenumbers                                                    */
+  const void* invKrsq;  /* nkr*ny, 1/(kr^2 + l^2) with the mean mode 0                       */
+  void* sol;            /* nkr*ny complex state, advanced in place                           */
+  void* buf[5];         /* ETDRK4: sol1, sol2, N1, N2, N3; RK4: sol1, RHS1, RHS2, RHS3;
+                           LSRK54: S2 -- nkr*ny complex each, owned by the caller            */
+  const void* coef[6];  /* ETDRK4: expLdt, exp_half_Ldt, zeta, alpha, beta, Gamma;
+                           RK4 / LSRK54: L -- nkr*ny real arrays (state precision)           */
+  const void* filter;   /* nkr*ny real filter of the Filtered* steppers, or NULL             */
+  double lsrk_A[5];     /* LSRK54 coefficients in the state precision (problem 0 is used)    */
+  double lsrk_B[5];
+} ff_vort_problem;
+
+/* Create a fused stepper for nprob problems (all of precision prec and one stepper kind).
+ * `filtered` applies each problem's filter at the end of the step as the Filtered*
+ * steppers do (src/timesteppers.jl:279,408,552).  The pointers in probs must stay valid
+ * for the handle's lifetime. */
+int ff_vort_create(int prec, int stepper, int filtered, double dt, int64_t nprob, const ff_vort_problem* probs,
+                   ff_vort** out);
+int ff_vort_destroy(ff_vort* h);
+
+/* Advance every problem nsteps steps on `stream` (no host synchronisation).  The first
+ * call captures a CUDA graph of one step (set FF_NO_GRAPH=1 to launch kernels directly). */
+int ff_vort_step(ff_vort* h, int64_t nsteps, void* stream);
+
+/* The bare nonlinear term N = calcN!(sol) of problem `prob` (nkr*ny complex each). */
+int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream);
+
+/* Launch geometry: cfg = {tile A, tile C, rows B, radix order, threads A, B, C, graph}. */
+int ff_vort_config(const ff_vort* h, int32_t cfg[8]);
+int ff_vort_set_config(ff_vort* h, int tla, int tlc, int tlr, int radix_variant);
+
+/* Time every tile / radix-order candidate for `steps_per_trial` steps and keep the
+ * fastest; the trial steps advance the state, so pass scratch states or restore them. */
+int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FOURIERFLOWS_GB300_H */

@@ -1,0 +1,155 @@
+"""The fused 2D vorticity path on the GPU against the CPU oracle.
+
+Tolerances: FP64 relative L2 <= 1e-12 over short horizons (the bar for the plain FP64
+path); FP32 state and transforms relative L2 <= 1e-5 against the FP64 oracle after
+100 steps."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import ff_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def make_pair(ff, n, stepper, T=np.float64, nu=1e-3, mu=1e-2, dt=2e-3, seed=3, af=1 / 3, ny=None, **kw):
+    ny = n if ny is None else ny
+    z0 = ff.Vorticity.random_phase_vorticity(n, ny, seed=seed, aliased_fraction=af if af > 0 else 1 / 3)
+    prob = ff.Vorticity.Problem(ff.GPU(), nx=n, ny=ny, Lx=2 * math.pi, nu=nu, mu=mu, dt=dt, stepper=stepper, T=T,
+                                aliased_fraction=af, **kw)
+    ff.Vorticity.set_zeta_(prob, z0)
+    g = orc.Grid(2, (n, ny), (2 * math.pi, 2 * math.pi), None, np.float64, af)
+    Lop = (-nu * g.Krsq - mu).astype(np.float64)
+    eq = orc.Equation(Lop, orc.vorticity_calcN, g)
+    oprob = orc.Problem(eq, stepper, dt, g, None, orc.VorticityParams(nu, mu), **kw)
+    oprob.sol[...] = orc.rfft(z0)
+    return prob, oprob
+
+
+@pytest.mark.parametrize("n,ny", [(32, 32), (64, 48), (128, 128), (48, 96)])
+def test_calcN_vs_oracle(ff, cuda, n, ny):
+    prob, oprob = make_pair(ff, n, "ETDRK4", ny=ny)
+    N = ff.zeros(ff.GPU(), np.complex128, (n // 2 + 1, ny))
+    ff.Vorticity.calcN_(N, prob.sol, 0.0, prob.clock, prob.vars, prob.params, prob.grid)
+    No = np.zeros_like(oprob.sol)
+    orc.vorticity_calcN(No, oprob.sol, 0.0, None, None, None, oprob.grid)
+    assert rel(ff.to_numpy(N), No) < 1e-13
+    # the input was not modified (the mask is applied on the fly)
+    assert np.array_equal(ff.to_numpy(prob.sol), oprob.sol) or rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-15
+
+
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredETDRK4", "RK4", "FilteredRK4", "LSRK54", "FilteredLSRK54"])
+def test_fused_steppers_vs_oracle_fp64(ff, cuda, stepper):
+    prob, oprob = make_pair(ff, 64, stepper)
+    assert prob.timestepper._native(prob.eqn) is not None, "expected the fused native stepper"
+    ff.stepforward_(prob, 10)
+    orc.stepforward(oprob, 10)
+    assert prob.clock.step == 10
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
+
+
+@pytest.mark.parametrize("stepper", ["ForwardEuler", "AB3", "FilteredAB3"])
+def test_generic_steppers_with_native_calcN(ff, cuda, stepper):
+    """Steppers without a fused path call the native calcN! between native substeps."""
+    prob, oprob = make_pair(ff, 32, stepper, dt=1e-3)
+    assert prob.timestepper._native(prob.eqn) is None
+    for _ in range(6):
+        ff.stepforward_(prob)
+    orc.stepforward(oprob, 6)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
+
+
+def test_nonsquare_radix3_grid(ff, cuda):
+    prob, oprob = make_pair(ff, 96, "ETDRK4", ny=48)
+    ff.stepforward_(prob, 5)
+    orc.stepforward(oprob, 5)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
+
+
+def test_no_dealiasing(ff, cuda):
+    prob, oprob = make_pair(ff, 32, "RK4", af=0)
+    ff.stepforward_(prob, 4)
+    orc.stepforward(oprob, 4)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
+
+
+def test_fp32_vs_fp64_oracle_100_steps(ff, cuda):
+    prob, oprob = make_pair(ff, 128, "ETDRK4", T=np.float32)
+    ff.stepforward_(prob, 100)
+    orc.stepforward(oprob, 100)
+    e = rel(ff.to_numpy(prob.sol).astype(np.complex128), oprob.sol)
+    assert e < 1e-5, e
+    E = ff.Vorticity.energy(prob)
+    Eo = orc.vorticity_energy(oprob.sol, oprob.grid)
+    assert abs(E - Eo) / Eo < 1e-5
+
+
+def test_energy_enstrophy_vs_oracle(ff, cuda):
+    prob, oprob = make_pair(ff, 64, "ETDRK4")
+    E, Z = ff.Vorticity.energy(prob), ff.Vorticity.enstrophy(prob)
+    assert abs(E - 0.5) < 1e-12  # the initial condition is normalised to E = 0.5
+    assert abs(E - orc.vorticity_energy(oprob.sol, oprob.grid)) < 1e-13
+    assert abs(Z - orc.vorticity_enstrophy(oprob.sol, oprob.grid)) / Z < 1e-13
+
+
+def test_updatevars(ff, cuda):
+    prob, oprob = make_pair(ff, 32, "ETDRK4")
+    ff.Vorticity.updatevars_(prob)
+    g = oprob.grid
+    zh = oprob.sol
+    psih = -zh * g.invKrsq
+    u = orc.irfft(-1j * g.l * psih, g.nx)
+    v = orc.irfft(1j * g.kr * psih, g.nx)
+    assert rel(ff.to_numpy(prob.vars.u), u) < 1e-13
+    assert rel(ff.to_numpy(prob.vars.v), v) < 1e-13
+    assert rel(ff.to_numpy(prob.vars.zeta), orc.irfft(zh, g.nx)) < 1e-13
+
+
+def test_full_size_1024_fp64_short_horizon(ff, cuda):
+    """The plain FP64 configuration (1024^2, nu=1e-4, mu=1e-2, dt=2e-3): 3 steps vs the oracle."""
+    prob, oprob = make_pair(ff, 1024, "ETDRK4", nu=1e-4, mu=1e-2, dt=2e-3, seed=2024)
+    ff.stepforward_(prob, 3)
+    orc.stepforward(oprob, 3)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
+
+
+def test_full_size_properties_1024(ff, cuda):
+    """Size-independent properties at 1024^2: the state stays 2/3-dealiased, energy decays
+    monotonically under viscosity + drag, and FP32 tracks FP64 on the GPU."""
+    p64, _ = make_pair(ff, 1024, "ETDRK4", nu=1e-4, mu=1e-2, dt=2e-3, seed=9)
+    p32, _ = make_pair(ff, 1024, "ETDRK4", T=np.float32, nu=1e-4, mu=1e-2, dt=2e-3, seed=9)
+    E = [ff.Vorticity.energy(p64)]
+    for _ in range(5):
+        ff.stepforward_(p64, 4)
+        ff.stepforward_(p32, 4)
+        E.append(ff.Vorticity.energy(p64))
+    assert all(b < a for a, b in zip(E, E[1:]))
+    s = ff.to_numpy(p64.sol)
+    g = p64.grid
+    assert np.abs(s[g.kralias.start:, :]).max() == 0
+    assert np.abs(s[:, g.lalias.start:g.lalias.stop]).max() == 0
+    assert rel(ff.to_numpy(p32.sol).astype(np.complex128), s) < 1e-5
+
+
+def test_autotune_keeps_results(ff, cuda):
+    """Every autotuner candidate computes the same step (tile shapes and radix orders
+    only change the schedule); the chosen configuration reproduces the oracle."""
+    prob, oprob = make_pair(ff, 64, "ETDRK4")
+    bound = prob.timestepper._native(prob.eqn)
+    fs = bound.ensure(prob.sol, prob.clock)
+    start = prob.sol.clone()
+    fs.autotune(steps_per_trial=1)
+    prob.sol.copy_(start)
+    ff.stepforward_(prob, 5)
+    orc.stepforward(oprob, 5)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
+    for cfg in [(1, 1, 1, 0), (4, 2, 4, 1), (2, 4, 2, 2)]:
+        fs.set_config(*cfg)
+        prob.sol.copy_(start)
+        fs.advance(5)
+        assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12, cfg
