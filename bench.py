@@ -1,0 +1,419 @@
+#!/usr/bin/env python
+"""ETDRK4 steps/s of the 2D vorticity problem on one GB300 (and N independent replicas).
+
+Workload (the plain FP64 configuration): TwoDGrid 1024 x 1024, Lx = Ly = 2 pi, Float64,
+L = -nu |k|^2 - mu with nu = 1e-4, mu = 1e-2, N = -J(psi, zeta) with 2/3 dealiasing,
+random-phase initial vorticity (seeded) with E(k) ~ k^4 exp(-2 (k/6)^2) and energy 0.5,
+ETDRK4 with dt = 2e-3.  A "step" is one ETDRK4 step of that problem.
+
+  value          steps/s with the state resident in HBM (device time, CUDA events around
+                 each step, L2 flushed between steps by writing a 256 MiB buffer)
+  e2e            steps/s through the public API (stepforward_) with the state copied from
+                 pinned host memory before every step and the energy read back after it
+  roofline       the dominant pass's algorithmic bytes (and FP64 flops) per launch over its
+                 event-timed duration, against the measured copy bandwidth (and FP64 rate)
+  cpu_baseline   the CPU oracle (numpy / scipy.fft, all host cores) on a bounded sample
+  forms          FP32 on the same problem, FP32 batched (32 problems of 1024^2 in one
+                 launch per pass) and the uneven ensemble (384 problems 128^2 .. 1024^2),
+                 with the FP32-vs-FP64 relative L2 error after 100 steps
+
+--impl reference times the CPU oracle of the same step (FourierFlows.jl itself is Julia,
+absent here) with every host thread.  Multi-GPU runs are independent replicas: each rank
+steps its own problem, there is no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, LX, NU, MU, DT, SEED = 1024, 2 * math.pi, 1e-4, 1e-2, 2e-3, 20260101
+METRIC = "ETDRK4 steps/s, 2D 1024²: FP32+batched vs FP64 plain @≤1e-5 rel L2; HBM GB/s"
+WORKLOAD = "2D vorticity ETDRK4, TwoDGrid 1024x1024 FP64, nu=1e-4, mu=1e-2, dt=2e-3, 2/3 dealiasing"
+
+
+def args_():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-forms", action="store_true", help="skip the FP32 / batched / ensemble forms")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--profile-case", default="", help="run only a small case for ncu (fp64|fp32|batch)")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------------------------------
+# helpers
+# ----------------------------------------------------------------------------------------
+def dist_init(gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def step_bytes_fp(n, es):
+    """Algorithmic bytes of one fused ETDRK4 step of an n^2 problem (es = bytes per complex):
+    every operand of every pass read once and every result written once."""
+    nkr = n // 2 + 1
+    nkd = math.floor((1 - 1 / 3) / 2 * n)  # kept kr columns
+    lrows = n - (math.ceil((1 + 1 / 3) / 2 * n) - nkd)  # kept l rows
+    rs = es // 2
+    C, Wd = nkr * n * es, nkd * n * es
+    a = nkd * lrows * (es + rs) + 3 * Wd       # zeta_hat + 1/K^2 (kept) -> W[3]
+    b = 3 * Wd + 2 * Wd                        # W[3] -> Q[2]
+    c1 = 2 * Wd + C + 2 * nkr * n * rs + 2 * C  # Q, sol, e_half, zeta -> N1, sol1
+    c3 = 2 * Wd + 2 * C + 2 * nkr * n * rs + 2 * C
+    c4 = 2 * Wd + 4 * C + 4 * nkr * n * rs + C
+    return {"A": a, "B": b, "C1": c1, "C3": c3, "C4": c4, "step": 4 * a + 4 * b + 2 * c1 + c3 + c4}
+
+
+def survey_step_bytes(n, s):
+    """20 (C + R) + 21 C with C = (n/2+1) n 2 s, R = n^2 s (one read + one write per FFT)."""
+    C = (n // 2 + 1) * n * 2 * s
+    R = n * n * s
+    return 20 * (C + R) + 21 * C
+
+
+def pass_flops(n):
+    """Nominal FFT flops per pass (5 N log2 N per complex, 2.5 N log2 N per real transform)."""
+    nkd = math.floor((1 - 1 / 3) / 2 * n)
+    lg = math.log2(n)
+    return {"A": 3 * nkd * 5 * n * lg, "B": n * 5 * 2.5 * n * lg, "C": 2 * nkd * 5 * n * lg}
+
+
+# ----------------------------------------------------------------------------------------
+# the reference arm: the CPU oracle of the same step
+# ----------------------------------------------------------------------------------------
+def cpu_oracle_rate(steps, warmup, budget_s, cores):
+    import numpy as np
+    from oracle import ff_oracle as orc
+    import fourierflows.jl_gb300.vorticity as vort
+    orc.set_workers(cores)
+    z0 = vort.random_phase_vorticity(N, seed=SEED)
+    prob = orc.VorticityProblem(N, LX, NU, MU, DT, "ETDRK4")
+    prob.sol[...] = orc.rfft(z0)
+    orc.stepforward(prob, max(1, warmup))
+    done, t0 = 0, time.perf_counter()
+    while done < steps:
+        orc.stepforward(prob, 1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, done, dt
+
+
+def reference_arm(a):
+    rank, world, _ = dist_init(a.gpus)
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    rate, done, secs = cpu_oracle_rate(a.steps, a.warmup, 150.0, cores)
+    line = {"metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": a.gpus, "steps": done, "warmup": a.warmup,
+            "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "parallelism": "cpu", "l2": "n/a"},
+            "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{done} ETDRK4 steps of the 1024^2 FP64 problem in {secs:.1f} s "
+                                       "(numpy/scipy.fft restatement of the reference; FourierFlows.jl is Julia, "
+                                       "absent on this box)"},
+            "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------------------
+def make_problem(ff, T):
+    import numpy as np
+    prob = ff.Vorticity.Problem(ff.GPU(), nx=N, Lx=LX, nu=NU, mu=MU, dt=DT, stepper="ETDRK4", T=T)
+    ff.Vorticity.set_zeta_(prob, ff.Vorticity.random_phase_vorticity(N, seed=SEED))
+    fs = prob.timestepper._native(prob.eqn).ensure(prob.sol, prob.clock)
+    return prob, fs
+
+
+def timed_steps(torch, fs, steps, flush):
+    """Sum of per-step device times (ms), L2 flushed before each step (not timed)."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for e0, e1 in ev:
+        flush.add_(1.0)
+        e0.record()
+        fs.advance(1)
+        e1.record()
+    torch.cuda.synchronize()
+    return sum(e0.elapsed_time(e1) for e0, e1 in ev)
+
+
+def autotune(torch, fs, sol):
+    saved = sol.clone()
+    fs.autotune(steps_per_trial=2)
+    sol.copy_(saved)
+    torch.cuda.synchronize()
+    return fs.config()
+
+
+def our_arm(a):
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import fourierflows.jl_gb300 as ff
+
+    rank, world, local = dist_init(a.gpus)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    pk = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    peak_src = "of measured" if "hbm_gbs" in pk else "of fallback"
+
+    prob, fs = make_problem(ff, np.float64)
+    cfg64 = autotune(torch, fs, prob.sol)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    fs.advance(a.warmup)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    total_ms = timed_steps(torch, fs, a.steps, flush)
+    torch.cuda.synchronize()
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    clk = clocks.stop()
+    ms_per_step = total_ms / a.steps
+    value = world * 1e3 / ms_per_step
+    launches = a.steps * 12
+
+    # per-pass device times (events inside the library) and the roofline of the dominant pass
+    tA, tB, tC = fs.profile(reps=20)
+    es = 16
+    bts = step_bytes_fp(N, es)
+    fl = pass_flops(N)
+    fp64 = ctypes_peak(ff)
+    passes = {"A": (tA, bts["A"], fl["A"]), "B": (tB, bts["B"], fl["B"]), "C": (tC, bts["C1"], fl["C"])}
+    dom = max(passes, key=lambda k: passes[k][0])
+    t_ms, byts, flops = passes[dom]
+    achieved = byts / (t_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": None, "kernel": f"k_vort_{dom.lower()} (pass {dom})", "peak_source": peak_src,
+                "pass_ms": {"A": tA, "B": tB, "C": tC},
+                "fp64": {"achieved_tflops": flops / (t_ms * 1e-3) / 1e12, "peak_tflops": fp64,
+                         "frac": (flops / (t_ms * 1e-3) / 1e12) / fp64 if fp64 else None,
+                         "peak_source": "measured by ff_fp64_peak in this run"}}
+
+    # end to end through the public API: pinned host state in, energy out, every step
+    host = torch.empty(prob.sol.shape[::-1], dtype=prob.sol.dtype, pin_memory=True).t()
+    host.copy_(prob.sol)
+    torch.cuda.synchronize()
+    e2e_steps = max(10, min(a.steps, 100))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        prob.sol.copy_(host, non_blocking=True)
+        ff.stepforward_(prob)
+        ff.Vorticity.energy(prob)  # device -> host read (8 bytes) and synchronisation
+    torch.cuda.synchronize()
+    e2e = world * e2e_steps / (time.perf_counter() - t0)
+    h2d = prob.sol.numel() * prob.sol.element_size()
+
+    forms = {} if a.no_forms else run_forms(torch, ff, a, hbm, peak_src)
+
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        cores = os.cpu_count() or 1
+        rate, done, secs = cpu_oracle_rate(6, 1, 20.0, cores)
+        cpu = {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": f"{done} ETDRK4 steps of the same 1024^2 FP64 problem in {secs:.1f} s (numpy/scipy.fft "
+                         "oracle, scipy workers = all host cores)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-phase vorticity)",
+                "config": {"workload": WORKLOAD, "global_batch": world, "parallelism": f"replicas{world}",
+                           "l2": "flushed between steps (256 MiB write)", "tiles": cfg64,
+                           "algorithmic_bytes_per_step": bts["step"],
+                           "survey_bytes_per_step": survey_step_bytes(N, 8)},
+                "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8},
+                "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "forms": forms}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def ctypes_peak(ff):
+    import ctypes as C
+    v = C.c_double()
+    try:
+        ff._lib.call("ff_fp64_peak", C.byref(v), None)
+        return v.value
+    except Exception:
+        return None
+
+
+def run_forms(torch, ff, a, hbm, peak_src):
+    import numpy as np
+    out = {}
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    steps = max(20, min(a.steps, 200))
+    # FP32 single problem and its accuracy against FP64 after 100 steps
+    p32, f32 = make_problem(ff, np.float32)
+    p64, f64s = make_problem(ff, np.float64)
+    f32.advance(100)
+    f64s.advance(100)
+    torch.cuda.synchronize()
+    s64 = ff.to_numpy(p64.sol)
+    s32 = ff.to_numpy(p32.sol).astype(np.complex128)
+    relL2 = float(np.linalg.norm(s32 - s64) / np.linalg.norm(s64))
+    E64, E32 = ff.Vorticity.energy(p64), ff.Vorticity.energy(p32)
+    Z64, Z32 = ff.Vorticity.enstrophy(p64), ff.Vorticity.enstrophy(p32)
+    del p64, f64s
+    cfg32 = autotune(torch, f32, p32.sol)
+    f32.advance(a.warmup)
+    ms32 = timed_steps(torch, f32, steps, flush) / steps
+    out["fp32_1024"] = {"value": 1e3 / ms32, "unit": "steps/s", "ms_per_step": ms32, "tiles": cfg32,
+                        "rel_l2_vs_fp64_after_100": relL2, "energy_rel_err": abs(E32 - E64) / E64,
+                        "enstrophy_rel_err": abs(Z32 - Z64) / Z64}
+    del p32, f32
+    # FP32 batched: 32 problems of 1024^2 advanced together
+    ens = ff.Vorticity.Ensemble([(N, NU, SEED + i) for i in range(32)], mu=MU, dt=DT, T=np.float32)
+    saved = [m.sol.clone() for m in ens.members]
+    ens.fs.autotune(steps_per_trial=1)
+    for m, s in zip(ens.members, saved):
+        m.sol.copy_(s)
+    ens.fs.advance(a.warmup)
+    bsteps = max(10, min(a.steps, 50))
+    msb = timed_steps(torch, ens.fs, bsteps, flush) / bsteps
+    tA, tB, tC = ens.fs.profile(reps=5)
+    bts = step_bytes_fp(N, 8)
+    passes = {"A": (tA, 32 * bts["A"]), "B": (tB, 32 * bts["B"]), "C": (tC, 32 * bts["C1"])}
+    dom = max(passes, key=lambda k: passes[k][0])
+    ach = passes[dom][1] / (passes[dom][0] * 1e-3) / 1e9
+    step_ach = 32 * bts["step"] / (msb * 1e-3) / 1e9
+    out["fp32_batched_1024x32"] = {
+        "value": 32 * 1e3 / msb, "unit": "problem-steps/s (1024^2 ETDRK4)", "ms_per_step": msb,
+        "tiles": ens.fs.config(), "l2": "working set 1.8 GB > L2; flushed between steps",
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                     "kernel": f"k_vort_{dom.lower()} (pass {dom})", "peak_source": peak_src,
+                     "pass_ms": {"A": tA, "B": tB, "C": tC}},
+        "step_algorithmic_gbs": step_ach, "step_frac": step_ach / hbm}
+    del ens, saved
+    # the uneven ensemble: 128 x 128^2, 128 x 256^2, 96 x 512^2, 32 x 1024^2, nu log-uniform
+    u = ff.Vorticity.uniform01(99, 384)
+    nus = 10 ** (-5 + 2 * u)
+    spec = [(128, nus[i], 1000 + i) for i in range(128)] + [(256, nus[128 + i], 2000 + i) for i in range(128)]
+    spec += [(512, nus[256 + i], 3000 + i) for i in range(96)] + [(1024, nus[352 + i], 4000 + i) for i in range(32)]
+    ens = ff.Vorticity.Ensemble(spec, mu=MU, dt=DT, T=np.float32)
+    ens.fs.advance(a.warmup)
+    msu = timed_steps(torch, ens.fs, bsteps, flush) / bsteps
+    gp = ens.grid_points
+    out["ensemble_uneven_384"] = {"value": 384 * 1e3 / msu, "unit": "problem-steps/s", "ms_per_step": msu,
+                                  "grid_point_steps_per_s": gp * 1e3 / msu, "problems": 384,
+                                  "sizes": "128x128^2 + 128x256^2 + 96x512^2 + 32x1024^2", "dtype": "f32"}
+    return out
+
+
+def profile_case(a):
+    """A small case for ncu: a few steps of one problem (fp64 / fp32) or a 4-problem batch."""
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import fourierflows.jl_gb300 as ff
+    torch.cuda.set_device(0)
+    if a.profile_case == "batch":
+        ens = ff.Vorticity.Ensemble([(N, NU, SEED + i) for i in range(4)], mu=MU, dt=DT, T=np.float32)
+        ens.fs.advance(a.steps)
+    else:
+        T = np.float64 if a.profile_case == "fp64" else np.float32
+        prob, fs = make_problem(ff, T)
+        fs.advance(a.steps)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": a.profile_case, "steps": a.steps}))
+
+
+if __name__ == "__main__":
+    A = args_()
+    if A.profile_case:
+        profile_case(A)
+    elif A.impl == "reference":
+        reference_arm(A)
+    else:
+        our_arm(A)

@@ -37,9 +37,48 @@ int elementwise_grid(int64_t n, int threads) {
   return (int)(g < 1 ? 1 : g);
 }
 
+// FP64 FMA throughput probe: 8 independent dependency chains per thread
+__global__ void k_fp64_fma(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
 }  // namespace ff
 
 extern "C" {
+
+int ff_fp64_peak(double* tflops, void* stream) {
+  FF_CHECK_ARG(tflops, "ff_fp64_peak: null output");
+  auto s = (cudaStream_t)stream;
+  double* d = nullptr;
+  FF_CUDA(cudaMalloc(&d, sizeof(double)));
+  const int threads = 256, blocks = ff::sm_count() * 8, iters = 4096;
+  cudaEvent_t e0, e1;
+  FF_CUDA(cudaEventCreate(&e0));
+  FF_CUDA(cudaEventCreate(&e1));
+  ff::k_fp64_fma<<<blocks, threads, 0, s>>>(d, iters, 0.999999, 1e-7);  // warm-up
+  FF_CUDA(cudaEventRecord(e0, s));
+  ff::k_fp64_fma<<<blocks, threads, 0, s>>>(d, iters, 0.999999, 1e-7);
+  FF_CUDA(cudaEventRecord(e1, s));
+  FF_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  FF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return FF_OK;
+}
 
 int ff_version(void) { return (0 << 16) | (1 << 8) | 0; }
 

@@ -260,8 +260,13 @@ template <typename T> __device__ __forceinline__ void r2c_pair(cx<T> zk, cx<T> z
 }
 
 // Inverse: 2 Z[k] = (X[k] + conj X[h-k]) + i conj(W_N^k) (X[k] - conj X[h-k]); the
-// unnormalised length-h inverse of 2Z is N times the packed real signal.
-template <typename T> __device__ __forceinline__ cx<T> c2r_pre(cx<T> xk, cx<T> xhk, cx<T> w) {
+// unnormalised length-h inverse of 2Z is N times the packed real signal.  At k = 0 only
+// the real parts of X[0] and X[h] enter, the projection onto real signals that FFTW's
+// and pocketfft's c2r make: a half spectrum whose kr = 0 column is not Hermitian (the
+// asymmetric 2/3 mask keeps l = -n/3 but not +n/3) then inverts to the real part of
+// the complex field it represents.
+template <typename T> __device__ __forceinline__ cx<T> c2r_pre(cx<T> xk, cx<T> xhk, cx<T> w, int k) {
+  if (k == 0) return mk<T>(xk.x + xhk.x, xk.x - xhk.x);
   cx<T> b = conj(xhk);
   return add(add(xk, b), mul_i(cmulc(sub(xk, b), w)));
 }

@@ -184,7 +184,7 @@ __global__ void k_c2r_rows(const cx<T>* __restrict__ in, T* __restrict__ out, in
     cx<T> v = czero<T>();
     if (row < nrows) {
       const cx<T>* r = in + row * nkr;
-      v = c2r_pre<T>(r[k], r[h - k], __ldg(&rtw[k]));
+      v = c2r_pre<T>(r[k], r[h - k], __ldg(&rtw[k]), k);
     }
     A[ad(ln, k)] = v;
   }

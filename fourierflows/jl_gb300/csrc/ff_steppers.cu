@@ -156,6 +156,63 @@ __global__ void k_mul_ik(int64_t n0, int64_t total, cx<T>* out, const cx<T>* in,
   GRID_STRIDE(i, total) out[i] = mul_i(scl(in[i], k[i % n0]));
 }
 
+// ---- ETDRK4 coefficients by the Kassam-Trefethen contour means, in FP64 ------------------
+// For each mode, z_j = dt L + r exp(2 pi i (j + 1/2) / M), j < M, and
+//   zeta  = dt mean((e^{z/2} - 1) / z)
+//   alpha = dt mean((-4 - z + e^z (4 - 3z + z^2)) / z^3)
+//   beta  = dt mean(( 2 + z + e^z (-2 + z)) / z^3)
+//   Gamma = dt mean((-4 - 3z - z^2 + e^z (4 - z)) / z^3)
+// (the reference's getetdcoeffs, src/timesteppers.jl:689-718; real parts for real L).
+struct Circle {
+  double2 c[64];
+  int m;
+};
+
+__device__ __forceinline__ double2 cexp64(double2 z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  const double e = exp(z.x);
+  return make_double2(e * c, e * s);
+}
+
+__device__ __forceinline__ double2 cdiv64(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+template <typename T>
+__global__ void k_etd_coefs(int64_t n, const T* __restrict__ L, T dt, Circle circ, T* zeta, T* alpha, T* beta,
+                            T* gamma) {
+  GRID_STRIDE(i, n) {
+    const double dtl = (double)(T)(dt * L[i]);  // dt L in L's precision, then FP64
+    double2 sz = make_double2(0, 0), sa = sz, sb = sz, sg = sz;
+    for (int j = 0; j < circ.m; ++j) {
+      const double2 z = make_double2(dtl + circ.c[j].x, circ.c[j].y);
+      const double2 ez = cexp64(z);
+      const double2 eh = cexp64(make_double2(0.5 * z.x, 0.5 * z.y));
+      const double2 z2 = cmul(z, z);
+      const double2 z3 = cmul(z2, z);
+      sz = add(sz, cdiv64(make_double2(eh.x - 1.0, eh.y), z));
+      // -4 - z + e^z (4 - 3z + z^2)
+      const double2 pa = add(make_double2(-4.0 - z.x, -z.y), cmul(ez, make_double2(4.0 - 3.0 * z.x + z2.x,
+                                                                                   -3.0 * z.y + z2.y)));
+      // 2 + z + e^z (-2 + z)
+      const double2 pb = add(make_double2(2.0 + z.x, z.y), cmul(ez, make_double2(-2.0 + z.x, z.y)));
+      // -4 - 3z - z^2 + e^z (4 - z)
+      const double2 pg = add(make_double2(-4.0 - 3.0 * z.x - z2.x, -3.0 * z.y - z2.y),
+                             cmul(ez, make_double2(4.0 - z.x, -z.y)));
+      sa = add(sa, cdiv64(pa, z3));
+      sb = add(sb, cdiv64(pb, z3));
+      sg = add(sg, cdiv64(pg, z3));
+    }
+    const double f = (double)dt / circ.m;
+    zeta[i] = (T)(f * sz.x);
+    alpha[i] = (T)(f * sa.x);
+    beta[i] = (T)(f * sb.x);
+    gamma[i] = (T)(f * sg.x);
+  }
+}
+
 // u_hat = i l zeta_hat / K^2, v_hat = -i kr zeta_hat / K^2 (psi_hat = -zeta_hat / K^2)
 template <typename T>
 __global__ void k_velocities(int64_t nkr, int64_t n, const cx<T>* __restrict__ zh, const T* __restrict__ kr,
@@ -422,6 +479,25 @@ int ff_parsevalsum2_weighted(int prec, const void* uh, const void* wt, int64_t n
   FF_PREC_DISPATCH(prec,
       return parseval<double>(uh, n0, nrest, rfft_form, 0, norm, out, (cudaStream_t)stream, wt, dev_out),
       return parseval<float>(uh, n0, nrest, rfft_form, 0, norm, out, (cudaStream_t)stream, wt, dev_out));
+  return FF_OK;
+}
+
+int ff_etdrk4_coefficients(int prec, int64_t n, const void* L, double dt, int ncirc, double rcirc, void* zeta,
+                           void* alpha, void* beta, void* gamma, void* stream) {
+  FF_CHECK_ARG(L && zeta && alpha && beta && gamma && n >= 1, "ff_etdrk4_coefficients: bad argument");
+  FF_CHECK_ARG(ncirc >= 1 && ncirc <= 64, "ff_etdrk4_coefficients: ncirc must be in 1..64");
+  Circle circ;
+  circ.m = ncirc;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int j = 0; j < ncirc; ++j) {
+    const long double a = 2.0L * pi * ((long double)j + 0.5L) / (long double)ncirc;
+    circ.c[j] = make_double2((double)(rcirc * cosl(a)), (double)(rcirc * sinl(a)));
+  }
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_etd_coefs<double>, n, n, (const double*)L, dt, circ, (double*)zeta, (double*)alpha, (double*)beta,
+               (double*)gamma),
+      LAUNCH1D(k_etd_coefs<float>, n, n, (const float*)L, (float)dt, circ, (float*)zeta, (float*)alpha, (float*)beta,
+               (float*)gamma));
   return FF_OK;
 }
 

@@ -499,6 +499,54 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   return FF_OK;
 }
 
+int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]) {
+  FF_CHECK_ARG(h && ms && reps >= 1, "ff_vort_profile: bad argument");
+  auto s = (cudaStream_t)stream;
+  cudaEvent_t ev[4];
+  for (auto& e : ev) FF_CUDA(cudaEventCreate(&e));
+  double acc[3] = {0, 0, 0};
+  int st = FF_OK;
+  for (int r = 0; r < reps && st == FF_OK; ++r) {
+    // pass A on the state, B, then C with the first substep's epilogue (which writes
+    // only the stepper's intermediate buffers for ETDRK4 and RK4)
+    FF_CUDA(cudaEventRecord(ev[0], s));
+    if (h->prec == FF_F64) {
+      const auto* P = (const VortProb<double>*)h->d_probs;
+      k_vort_a<double><<<h->g.ga, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)h->d_work_a, h->nwork_a, h->g.tla,
+                                                            (const double2* const*)h->d_inputs);
+      FF_CUDA(cudaEventRecord(ev[1], s));
+      k_vort_b<double><<<h->g.gb, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)h->d_work_b, h->nwork_b, h->g.tlr);
+      FF_CUDA(cudaEventRecord(ev[2], s));
+      EpiScalars<double> S{};
+      S.c = h->dt / 2;
+      st = h->stepper == FF_STEP_RK4 ? launch_c<double, EPI_RK1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s)
+                                     : launch_c<double, EPI_ETD1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
+    } else {
+      const auto* P = (const VortProb<float>*)h->d_probs;
+      k_vort_a<float><<<h->g.ga, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)h->d_work_a, h->nwork_a, h->g.tla,
+                                                           (const float2* const*)h->d_inputs);
+      FF_CUDA(cudaEventRecord(ev[1], s));
+      k_vort_b<float><<<h->g.gb, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)h->d_work_b, h->nwork_b, h->g.tlr);
+      FF_CUDA(cudaEventRecord(ev[2], s));
+      EpiScalars<float> S{};
+      S.c = (float)(h->dt / 2);
+      st = h->stepper == FF_STEP_RK4 ? launch_c<float, EPI_RK1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s)
+                                     : launch_c<float, EPI_ETD1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
+    }
+    FF_LAUNCHED("ff_vort_profile");
+    FF_CUDA(cudaEventRecord(ev[3], s));
+    FF_CUDA(cudaEventSynchronize(ev[3]));
+    for (int k = 0; k < 3; ++k) {
+      float t = 0;
+      FF_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      acc[k] += t;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int k = 0; k < 3; ++k) ms[k] = acc[k] / reps;
+  return st;
+}
+
 int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream) {
   FF_CHECK_ARG(h && sol && N, "ff_vort_calcN: null argument");
   FF_CHECK_ARG(prob >= 0 && prob < h->nprob, "ff_vort_calcN: problem index out of range");

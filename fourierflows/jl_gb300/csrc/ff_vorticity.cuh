@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(512) k_vort_b(const VortProb<T>* __restrict__ 
         const cx<T>* src = P.W + f * fstride + (int64_t)j * nkd;
         const cx<T> xk = k < nkd ? src[k] : czero<T>();
         const cx<T> xh = (h - k) < nkd ? src[h - k] : czero<T>();
-        v = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]));
+        v = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]), k);
       }
       b[f][ad(ln, k)] = v;
     }

@@ -273,7 +273,11 @@ def getetdcoeffs(dt, L, ncirc=32, rcirc=1):
         dtL = (L.dtype.type(dt) * L).astype(L.dtype)
     else:
         dtL = np.asarray(type(dt)(dt) * L)
-    zc = np.asarray(dtL)[..., None].astype(np.complex128) + circ
+    return _etd_contour(np.asarray(dtL), dt, circ, L.dtype.kind != "c")
+
+
+def _etd_contour(dtL, dt, circ, real):
+    zc = dtL[..., None].astype(np.complex128) + circ
     ez, ez2 = np.exp(zc), np.exp(zc / 2)
     zeta = (ez2 - 1) / zc
     alpha = (-4 - zc + ez * (4 - 3 * zc + zc ** 2)) / zc ** 3
@@ -281,7 +285,7 @@ def getetdcoeffs(dt, L, ncirc=32, rcirc=1):
     gamma = (-4 - 3 * zc - zc ** 2 + ez * (4 - zc)) / zc ** 3
     dt64 = np.float64(dt)
     out = [dt64 * c.mean(axis=-1) for c in (zeta, alpha, beta, gamma)]
-    if L.dtype.kind != "c":
+    if real:
         out = [np.real(c) for c in out]
     return tuple(out)
 

@@ -116,6 +116,12 @@ class FusedStepper:
     def calcN(self, N, sol, prob=0, stream=None):
         _lib.call("ff_vort_calcN", self._h, int(prob), ptr(sol, "sol"), ptr(N, "N"), stream_handle(stream))
 
+    def profile(self, reps=10, stream=None):
+        """Average device ms of passes A, B, C (CUDA events inside the library)."""
+        ms = (C.c_double * 3)()
+        _lib.call("ff_vort_profile", self._h, int(reps), stream_handle(stream), ms)
+        return tuple(ms)
+
 
 def _stepper_struct(ts, eq, sol):
     """Fill an ff_vort_problem from a TimeStepper's buffers and coefficients (or None)."""
@@ -368,3 +374,104 @@ def random_phase_vorticity(nx, ny=None, Lx=2 * math.pi, Ly=None, seed=1234, k0=6
         w[-1] = 1.0
     E = 0.5 * np.sum(w[:, None] * np.abs(zr) ** 2 * invK2) / (nx * ny) ** 2
     return np.asfortranarray(zeta * math.sqrt(E0 / E))
+
+
+# ----------------------------------------------------------------------------------------
+# ensembles
+# ----------------------------------------------------------------------------------------
+class EnsembleMember:
+    """State, stepper buffers and coefficients of one ensemble problem (device arrays)."""
+
+    def __init__(self, grid, nu, mu, dt, stepper, T):
+        from .timesteppers import getetdcoeffs
+        self.grid, self.nu, self.mu = grid, nu, mu
+        Tf = np.dtype(T).type
+        Ct = cxtype(T)
+        shape = (grid.nkr, grid.ny)
+        dev = grid.device
+        L = (-nu * grid.Krsq_host.astype(np.float64) - mu).astype(Tf)
+        self.sol = zeros(dev, Ct, shape)
+        up = device_array(dev)
+        self.L = up(L)
+        self.kind = stepper.replace("Filtered", "")
+        if self.kind == "ETDRK4":
+            dtT = Tf(dt)
+            dtL = (dtT * L).astype(Tf)
+            self.coefs = [up(np.exp(dtL).astype(Tf)), up(np.exp((dtL / Tf(2)).astype(Tf)).astype(Tf))]
+            # zeta, alpha, beta, Gamma: the 32-point contour means evaluated in FP64 on the GPU
+            zab = [zeros(dev, Tf, shape) for _ in range(4)]
+            _lib.call("ff_etdrk4_coefficients", prec_of(self.L.dtype), self.L.numel(), ptr(self.L), float(dtT), 32,
+                      1.0, ptr(zab[0]), ptr(zab[1]), ptr(zab[2]), ptr(zab[3]), stream_handle())
+            self.coefs += zab
+            self.bufs = [zeros(dev, Ct, shape) for _ in range(5)]
+        elif self.kind == "RK4":
+            self.coefs = [self.L]
+            self.bufs = [zeros(dev, Ct, shape) for _ in range(4)]
+        elif self.kind == "LSRK54":
+            self.coefs = [self.L]
+            self.bufs = [zeros(dev, Ct, shape)]
+        else:
+            raise ValueError(f"the ensemble path supports ETDRK4, RK4 and LSRK54 (got {stepper})")
+        self.filter = None
+        if stepper.startswith("Filtered"):
+            from .domains import makefilter_host
+            self.filter = up(makefilter_host(grid, shape, order=4, innerK=0.65).astype(Tf))
+
+
+class Ensemble:
+    """Independent 2D vorticity problems of (possibly) different sizes advanced together:
+    every substep is three persistent launches over all members and a step is one CUDA
+    graph replay.  ``members`` are (n, nu, seed) triples; grids of equal size share their
+    wavenumber arrays.  ``value`` counters are problem-steps."""
+
+    def __init__(self, members, mu=1e-2, dt=2e-3, stepper="ETDRK4", T=np.float32, Lx=2 * math.pi, E0=0.5,
+                 k0=6.0, dev=None):
+        from .timesteppers import _LSRK_A, _LSRK_B
+        dev = dev if dev is not None else GPU()
+        self.T, self.dt, self.stepper = np.dtype(T).type, dt, stepper
+        self.grids = {}
+        self.members = []
+        structs, keep = [], []
+        for (n, nu, seed) in members:
+            g = self.grids.get(n)
+            if g is None:
+                g = TwoDGrid(dev, nx=n, Lx=Lx, T=T)
+                self.grids[n] = g
+            m = EnsembleMember(g, nu, mu, dt, stepper, T)
+            z0 = random_phase_vorticity(n, seed=seed, k0=k0, E0=E0)
+            zd = device_array(dev)(z0.astype(self.T))
+            mul_(m.sol, g.rfftplan, zd)
+            m.seed = seed
+            self.members.append(m)
+            q = _vort_problem_struct(g, m.sol)
+            for i, b in enumerate(m.bufs):
+                q.buf[i] = ptr(b).value
+            for i, c in enumerate(m.coefs):
+                q.coef[i] = ptr(c).value
+            if m.filter is not None:
+                q.filter = ptr(m.filter).value
+            Tf = self.T
+            for i in range(5):
+                q.lsrk_A[i] = float(Tf(float(_LSRK_A[i])))
+                q.lsrk_B[i] = float(Tf(float(_LSRK_B[i])))
+            structs.append(q)
+            keep += [m, g]
+        kind = stepper.replace("Filtered", "")
+        self.fs = FusedStepper(kind, stepper.startswith("Filtered"), dt, prec_of(self.members[0].sol.dtype), structs,
+                               keep)
+        self.step = 0
+
+    def stepforward_(self, nsteps=1, stream=None):
+        self.fs.advance(nsteps, stream)
+        self.step += nsteps
+
+    @property
+    def grid_points(self):
+        return sum(m.grid.nx * m.grid.ny for m in self.members)
+
+    def energies(self):
+        out = []
+        for m in self.members:
+            g = m.grid
+            out.append(0.5 * _weighted(m.sol, g, g.invKrsq) / (float(g.Lx) * float(g.Ly)))
+        return out

@@ -59,6 +59,10 @@ typedef struct {
 int ff_version(void);                       /* (major << 16) | (minor << 8) | patch        */
 int ff_last_error(char* buf, size_t len);   /* copies the calling thread's last message   */
 
+/* FP64 FMA throughput of the current device (TFLOP/s, one timed launch): the ceiling of
+ * the FP64 transforms, which on this part are FP64-pipe bound rather than HBM bound. */
+int ff_fp64_peak(double* tflops, void* stream);
+
 /* ---- FFT plans ----------------------------------------------------------------------- */
 typedef struct ff_plan ff_plan;
 
@@ -134,6 +138,14 @@ int ff_etdrk4_update(int prec, int64_t n, void* sol, ff_coef expL, ff_coef alpha
  * dt (23/12 RHS - 16/12 RHSm1 + 5/12 RHSm2); [sol *= filter]; RHSm2 = RHSm1; RHSm1 = RHS */
 int ff_ab3_update(int prec, int64_t n, void* sol, void* RHS, void* RHSm1, void* RHSm2, ff_coef L, double dt,
                   int euler, const void* filter, void* stream);
+
+/* The ETDRK4 coefficients zeta, alpha, beta, Gamma of a real linear operator L (n values,
+ * state precision) for step dt, by the ncirc-point contour means of getetdcoeffs
+ * (src/timesteppers.jl:689-718, ncirc = 32, rcirc = 1 there), evaluated in FP64 on the
+ * device and rounded to the state precision.  Used to set up large ensembles; the
+ * drop-in ETDRK4TimeStepper computes them on the host as the reference does. */
+int ff_etdrk4_coefficients(int prec, int64_t n, const void* L, double dt, int ncirc, double rcirc, void* zeta,
+                           void* alpha, void* beta, void* gamma, void* stream);
 
 /* sol .*= filter (src/timesteppers.jl:279,408,552,658) */
 int ff_filter_mul(int prec, int64_t n, void* sol, const void* filter, void* stream);
@@ -213,6 +225,11 @@ int ff_vort_step(ff_vort* h, int64_t nsteps, void* stream);
 
 /* The bare nonlinear term N = calcN!(sol) of problem `prob` (nkr*ny complex each). */
 int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream);
+
+/* Average device time (ms) of each of the three passes over `reps` launches, timed with
+ * CUDA events on `stream`: ms = {A, B, C}; C runs the first substep's epilogue, which for
+ * ETDRK4 and RK4 writes only the stepper's intermediate buffers. */
+int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]);
 
 /* Launch geometry: cfg = {tile A, tile C, rows B, radix order, threads A, B, C, graph}. */
 int ff_vort_config(const ff_vort* h, int32_t cfg[8]);
