@@ -77,6 +77,7 @@ SIGNATURES = {
     "ff_vort_profile": [vp, i32, vp, C.POINTER(f64)],
     "ff_etdrk4_coefficients": [i32, i64, vp, f64, i32, f64, vp, vp, vp, vp, vp],
     "ff_fp64_peak": [C.POINTER(f64), vp],
+    "ff_parsevalsum2_noalloc": [i32, vp, i64, i64, i32, f64, vp, vp],
 }
 
 FF_STEP_ETDRK4, FF_STEP_RK4, FF_STEP_LSRK54 = 0, 1, 2

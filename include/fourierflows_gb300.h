@@ -174,6 +174,17 @@ int ff_parsevalsum(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft
 int ff_parsevalsum2_weighted(int prec, const void* uh, const void* wt, int64_t n0, int64_t nrest, int rfft_form,
                              double norm, double* out, double* dev_out, void* stream);
 
+/* parsevalsum2 that allocates no device memory.  No counterpart in the reference: it
+ * serves callers that cannot call cudaMalloc because another allocator owns the GPU's
+ * memory (a pooling allocator that has reserved it, or a fixed-budget embedded code).
+ * The caller passes uh and a device double `out` (written on `stream`, no host
+ * synchronisation); the scratch is a 32 KiB static device array, so n0 * nrest is limited
+ * to 33,554,432 modes (larger sizes return FF_ERR_ARG).  The first call on each device
+ * looks up that array's device address; make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race. */
+int ff_parsevalsum2_noalloc(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft_form, double norm,
+                            double* out, void* stream);
+
 /* u_hat = -i l psi_hat, v_hat = i kr psi_hat with psi_hat = -zeta_hat invKrsq on the
  * (nkr, ny) half spectrum: the velocity spectra of a vorticity field. */
 int ff_vort_velocities(int prec, int64_t nkr, int64_t ny, const void* zh, const void* kr, const void* l,
