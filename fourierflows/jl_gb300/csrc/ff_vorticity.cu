@@ -14,11 +14,19 @@ namespace {
 
 struct Geom {
   int tla = 0, tlc = 0, tlr = 0;   // tile widths of passes A, C and rows per CTA of pass B
+                                   // (register path: lines per CTA of the largest problem)
   int tha = 0, thb = 0, thc = 0;   // threads per CTA
   size_t sma = 0, smb = 0, smc = 0;
   int ga = 0, gb = 0, gc = 0;      // grid sizes
-  int radix_variant = 0;           // 0: radix-8 first, 1: radix-4 first, 2: small radix first
+  int radix_variant = 0;           // generic path: 0 radix-8 first, 1 radix-4 first, 2 small radix first
+  bool reg = false;                // register-resident power-of-two kernels
 };
+
+int pow2_floor(int v) {
+  int p = 1;
+  while (p * 2 <= v) p *= 2;
+  return p;
+}
 
 // factorisation variants explored by the autotuner
 bool factorize_variant(int n, int variant, LinePlan& P) {
@@ -83,7 +91,51 @@ namespace {
 
 template <typename T> size_t elem() { return sizeof(cx<T>); }
 
+bool reg_capable(const ff_vort* h) {
+  const char* gen = getenv("FF_VORT_GENERIC");
+  if (gen && gen[0] == '1') return false;
+  for (const auto& q : h->host)
+    if (!regfft_ok((int)q.ny) || !regfft_ok((int)(q.nx / 2)) || q.nx / 2 > 2048) return false;
+  return true;
+}
+
+template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, int tlr) {
+  Geom g;
+  g.reg = true;
+  const size_t es = elem<T>();
+  const int ny = h->max_ny, hx = h->max_nx / 2;
+  const bool f64 = sizeof(T) == 8;
+  g.tla = tla > 0 ? tla : (f64 ? 2 : 4);
+  g.tlc = tlc > 0 ? tlc : (f64 ? 2 : 4);
+  g.tlr = tlr > 0 ? tlr : (f64 ? 2 : 4);
+  auto threads = [](int lines, int n, int cap) {
+    int t = pow2_floor(std::max(1, lines)) * (n / 8);
+    t = std::max(t, n / 8);
+    t = std::max(t, 32);
+    while (t > cap && t > n / 8) t /= 2;
+    return t;
+  };
+  g.tha = threads(g.tla, ny, 512);
+  g.thc = threads(g.tlc, ny, 512);
+  g.thb = threads(g.tlr, hx, 256);
+  g.tla = g.tha * 8 / ny;
+  g.tlc = g.thc * 8 / ny;
+  g.tlr = g.thb * 8 / hx;
+  g.sma = 9 * (size_t)g.tha * es;
+  g.smc = 2 * 9 * (size_t)g.thc * es;
+  size_t smb = 0;
+  const int sh = f64 ? 3 : 4;
+  for (const auto& q : h->host) {
+    const int H = (int)(q.nx / 2);
+    const size_t rows = (size_t)g.thb * 8 / H;
+    smb = std::max(smb, 3 * rows * (size_t)(H + (H >> sh) + 1) * es);
+  }
+  g.smb = smb;
+  return g;
+}
+
 template <typename T> Geom choose_geom(const ff_vort* h, int tla, int tlc, int tlr, int variant) {
+  if (reg_capable(h)) return choose_geom_reg<T>(h, tla, tlc, tlr);
   Geom g;
   const int ny = h->max_ny, hx = h->max_nx / 2;
   const size_t es = elem<T>();
@@ -182,12 +234,17 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
     } else {
       P.s1 = (cx<T>*)q.buf[0];
     }
-    const int ta = (int)ceil_div(P.nkd, geom.tla);
+    // tile widths: fixed on the generic path; on the register path a CTA holds
+    // threads*8 elements, i.e. threads*8/N lines of this problem's length N
+    const int wa_ = geom.reg ? geom.tha * 8 / P.ny : geom.tla;
+    const int wb_ = geom.reg ? geom.thb * 8 / (P.nx / 2) : geom.tlr;
+    const int wc_ = geom.reg ? geom.thc * 8 / P.ny : geom.tlc;
+    const int ta = (int)ceil_div(P.nkd, wa_);
     for (int f = 0; f < 3; ++f)
       for (int tt = 0; tt < ta; ++tt) wa.push_back({(int)i, tt, f, 0});
-    const int tb = (int)ceil_div(P.ny, geom.tlr);
+    const int tb = (int)ceil_div(P.ny, wb_);
     for (int tt = 0; tt < tb; ++tt) wb.push_back({(int)i, tt, 0, 0});
-    const int tc = (int)ceil_div(P.nkr, geom.tlc);
+    const int tc = (int)ceil_div(P.nkr, wc_);
     for (int tt = 0; tt < tc; ++tt) wc.push_back({(int)i, tt, 0, 0});
   }
   // longest work first helps the persistent grid balance uneven sizes
@@ -228,25 +285,54 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   FF_CUDA(cudaMalloc(&h->d_inputs, sizeof(void*) * in.size()));
   FF_CUDA(cudaMemcpy(h->d_inputs, in.data(), sizeof(void*) * in.size(), cudaMemcpyHostToDevice));
   h->g = geom;
-  if (int st = ensure_smem((const void*)k_vort_a<T>, geom.sma)) return st;
-  if (int st = ensure_smem((const void*)k_vort_b<T>, geom.smb)) return st;
-#define FF_SMEM_C(E) if (int st = ensure_smem((const void*)k_vort_c<T, E>, geom.smc)) return st;
+  const void* ka = geom.reg ? (const void*)k_vort_a_r<T> : (const void*)k_vort_a<T>;
+  const void* kb = geom.reg ? (const void*)k_vort_b_r<T> : (const void*)k_vort_b<T>;
+  if (int st = ensure_smem(ka, geom.sma)) return st;
+  if (int st = ensure_smem(kb, geom.smb)) return st;
+#define FF_SMEM_C(E)                                                                                       \
+  if (int st = ensure_smem(geom.reg ? (const void*)k_vort_c_r<T, E> : (const void*)k_vort_c<T, E>, geom.smc)) \
+    return st;
   FF_SMEM_C(EPI_N) FF_SMEM_C(EPI_ETD1) FF_SMEM_C(EPI_ETD2) FF_SMEM_C(EPI_ETD3) FF_SMEM_C(EPI_ETD4)
   FF_SMEM_C(EPI_RK1) FF_SMEM_C(EPI_RK2) FF_SMEM_C(EPI_RK3) FF_SMEM_C(EPI_RK4) FF_SMEM_C(EPI_LS)
 #undef FF_SMEM_C
-  h->g.ga = grid_for<T>((const void*)k_vort_a<T>, geom.tha, geom.sma, h->nwork_a);
-  h->g.gb = grid_for<T>((const void*)k_vort_b<T>, geom.thb, geom.smb, h->nwork_b);
-  h->g.gc = grid_for<T>((const void*)k_vort_c<T, EPI_ETD1>, geom.thc, geom.smc, h->nwork_c);
+  h->g.ga = grid_for<T>(ka, geom.tha, geom.sma, h->nwork_a);
+  h->g.gb = grid_for<T>(kb, geom.thb, geom.smb, h->nwork_b);
+  h->g.gc = grid_for<T>(geom.reg ? (const void*)k_vort_c_r<T, EPI_ETD1> : (const void*)k_vort_c<T, EPI_ETD1>,
+                        geom.thc, geom.smc, h->nwork_c);
   if (h->exec) { cudaGraphExecDestroy(h->exec); h->exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  return FF_OK;
+}
+
+// launches of one pass over a descriptor array and work list (generic or register path)
+template <typename T>
+int launch_a(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, const void* inputs,
+             cudaStream_t s) {
+  const auto* P = (const VortProb<T>*)probs;
+  if (h->g.reg)
+    k_vort_a_r<T><<<grid, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)work, nwork, (const cx<T>* const*)inputs);
+  else
+    k_vort_a<T><<<grid, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)work, nwork, h->g.tla,
+                                                 (const cx<T>* const*)inputs);
+  FF_LAUNCHED("k_vort_a");
+  return FF_OK;
+}
+
+template <typename T>
+int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, cudaStream_t s) {
+  const auto* P = (const VortProb<T>*)probs;
+  if (h->g.reg) k_vort_b_r<T><<<grid, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)work, nwork);
+  else k_vort_b<T><<<grid, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)work, nwork, h->g.tlr);
+  FF_LAUNCHED("k_vort_b");
   return FF_OK;
 }
 
 template <typename T, int EPI>
 int launch_c(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, EpiScalars<T> S,
              cudaStream_t s) {
-  k_vort_c<T, EPI><<<grid, h->g.thc, h->g.smc, s>>>((const VortProb<T>*)probs, (const WorkItem*)work, nwork,
-                                                     h->g.tlc, S);
+  const auto* P = (const VortProb<T>*)probs;
+  if (h->g.reg) k_vort_c_r<T, EPI><<<grid, h->g.thc, h->g.smc, s>>>(P, (const WorkItem*)work, nwork, S);
+  else k_vort_c<T, EPI><<<grid, h->g.thc, h->g.smc, s>>>(P, (const WorkItem*)work, nwork, h->g.tlc, S);
   FF_LAUNCHED("k_vort_c");
   return FF_OK;
 }
@@ -254,12 +340,8 @@ int launch_c(const ff_vort* h, const void* probs, const void* work, int nwork, i
 // one calcN! (passes A, B, C) with epilogue EPI on all problems; `inputs` = pass-A sources
 template <typename T, int EPI>
 int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s) {
-  const auto* P = (const VortProb<T>*)h->d_probs;
-  k_vort_a<T><<<h->g.ga, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)h->d_work_a, h->nwork_a, h->g.tla,
-                                                   (const cx<T>* const*)inputs);
-  FF_LAUNCHED("k_vort_a");
-  k_vort_b<T><<<h->g.gb, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)h->d_work_b, h->nwork_b, h->g.tlr);
-  FF_LAUNCHED("k_vort_b");
+  if (int st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, inputs, s)) return st;
+  if (int st = launch_b<T>(h, h->d_probs, h->d_work_b, h->nwork_b, h->g.gb, s)) return st;
   return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
 }
 
@@ -435,7 +517,7 @@ int ff_vort_config(const ff_vort* h, int32_t cfg[8]) {
   cfg[0] = h->g.tla;
   cfg[1] = h->g.tlc;
   cfg[2] = h->g.tlr;
-  cfg[3] = h->g.radix_variant;
+  cfg[3] = h->g.reg ? -1 : h->g.radix_variant;  // -1: register-resident power-of-two path
   cfg[4] = h->g.tha;
   cfg[5] = h->g.thb;
   cfg[6] = h->g.thc;
@@ -455,17 +537,19 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   // The trial steps advance the state: callers pass a scratch copy or restore it.
   auto s = (cudaStream_t)stream;
   const int reps = steps_per_trial > 0 ? steps_per_trial : 3;
-  const int tls_f64[] = {1, 2, 4};
+  const int tls_f64[] = {1, 2, 4, 8};
   const int tls_f32[] = {1, 2, 4, 8};
+  // the register path has one stage schedule; only the generic path varies radix order
+  const int nvar = reg_capable(h) ? 1 : 3;
   const int* tls = h->prec == FF_F64 ? tls_f64 : tls_f32;
-  const int ntl = h->prec == FF_F64 ? 3 : 4;
+  const int ntl = 4;
   double best = 1e30;
   int bcfg[4] = {0, 0, 0, 0};
   cudaEvent_t e0, e1;
   FF_CUDA(cudaEventCreate(&e0));
   FF_CUDA(cudaEventCreate(&e1));
   int st = FF_OK;
-  for (int v = 0; v < 3 && st == FF_OK; ++v)
+  for (int v = 0; v < nvar && st == FF_OK; ++v)
     for (int ia = 0; ia < ntl && st == FF_OK; ++ia)
       for (int ic = 0; ic < ntl && st == FF_OK; ++ic)
         for (int ir = 0; ir < ntl && st == FF_OK; ++ir) {
@@ -499,41 +583,26 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   return FF_OK;
 }
 
-int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]) {
-  FF_CHECK_ARG(h && ms && reps >= 1, "ff_vort_profile: bad argument");
-  auto s = (cudaStream_t)stream;
+}  // extern "C"
+
+template <typename T> int profile_t(ff_vort* h, int reps, cudaStream_t s, double ms[3]) {
   cudaEvent_t ev[4];
   for (auto& e : ev) FF_CUDA(cudaEventCreate(&e));
   double acc[3] = {0, 0, 0};
   int st = FF_OK;
+  EpiScalars<T> S{};
+  S.c = (T)(h->dt / 2);
   for (int r = 0; r < reps && st == FF_OK; ++r) {
     // pass A on the state, B, then C with the first substep's epilogue (which writes
     // only the stepper's intermediate buffers for ETDRK4 and RK4)
     FF_CUDA(cudaEventRecord(ev[0], s));
-    if (h->prec == FF_F64) {
-      const auto* P = (const VortProb<double>*)h->d_probs;
-      k_vort_a<double><<<h->g.ga, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)h->d_work_a, h->nwork_a, h->g.tla,
-                                                            (const double2* const*)h->d_inputs);
-      FF_CUDA(cudaEventRecord(ev[1], s));
-      k_vort_b<double><<<h->g.gb, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)h->d_work_b, h->nwork_b, h->g.tlr);
-      FF_CUDA(cudaEventRecord(ev[2], s));
-      EpiScalars<double> S{};
-      S.c = h->dt / 2;
-      st = h->stepper == FF_STEP_RK4 ? launch_c<double, EPI_RK1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s)
-                                     : launch_c<double, EPI_ETD1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
-    } else {
-      const auto* P = (const VortProb<float>*)h->d_probs;
-      k_vort_a<float><<<h->g.ga, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)h->d_work_a, h->nwork_a, h->g.tla,
-                                                           (const float2* const*)h->d_inputs);
-      FF_CUDA(cudaEventRecord(ev[1], s));
-      k_vort_b<float><<<h->g.gb, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)h->d_work_b, h->nwork_b, h->g.tlr);
-      FF_CUDA(cudaEventRecord(ev[2], s));
-      EpiScalars<float> S{};
-      S.c = (float)(h->dt / 2);
-      st = h->stepper == FF_STEP_RK4 ? launch_c<float, EPI_RK1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s)
-                                     : launch_c<float, EPI_ETD1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
-    }
-    FF_LAUNCHED("ff_vort_profile");
+    if ((st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, h->d_inputs, s))) break;
+    FF_CUDA(cudaEventRecord(ev[1], s));
+    if ((st = launch_b<T>(h, h->d_probs, h->d_work_b, h->nwork_b, h->g.gb, s))) break;
+    FF_CUDA(cudaEventRecord(ev[2], s));
+    st = h->stepper == FF_STEP_RK4 ? launch_c<T, EPI_RK1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s)
+                                   : launch_c<T, EPI_ETD1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
+    if (st) break;
     FF_CUDA(cudaEventRecord(ev[3], s));
     FF_CUDA(cudaEventSynchronize(ev[3]));
     for (int k = 0; k < 3; ++k) {
@@ -547,36 +616,33 @@ int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]) {
   return st;
 }
 
-int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream) {
-  FF_CHECK_ARG(h && sol && N, "ff_vort_calcN: null argument");
-  FF_CHECK_ARG(prob >= 0 && prob < h->nprob, "ff_vort_calcN: problem index out of range");
+extern "C" int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]) {
+  FF_CHECK_ARG(h && ms && reps >= 1, "ff_vort_profile: bad argument");
   auto s = (cudaStream_t)stream;
-  // single-problem descriptor copy with sol -> input and n1 -> N, and its work lists
-  const bool f64 = h->prec == FF_F64;
-  const size_t psz = f64 ? sizeof(VortProb<double>) : sizeof(VortProb<float>);
-  std::vector<unsigned char> desc(h->host_desc.begin() + psz * prob, h->host_desc.begin() + psz * (prob + 1));
-  int nx, ny, nkd, nkr;
-  if (f64) {
-    auto* P = (VortProb<double>*)desc.data();
-    P->n1 = (double2*)N;
-    nx = P->nx; ny = P->ny; nkd = P->nkd; nkr = P->nkr;
-  } else {
-    auto* P = (VortProb<float>*)desc.data();
-    P->n1 = (float2*)N;
-    nx = P->nx; ny = P->ny; nkd = P->nkd; nkr = P->nkr;
-  }
-  (void)nx;
+  return h->prec == FF_F64 ? profile_t<double>(h, reps, s, ms) : profile_t<float>(h, reps, s, ms);
+}
+
+template <typename T> int calcN_t(ff_vort* h, int64_t prob, const void* sol, void* N, cudaStream_t s) {
+  // a single-problem copy of descriptor `prob` with n1 -> N, its own work lists and the
+  // input pointer, staged through a persistent host buffer and copied on the stream
+  const size_t psz = sizeof(VortProb<T>);
+  VortProb<T> P;
+  memcpy(&P, h->host_desc.data() + psz * prob, psz);
+  P.n1 = (cx<T>*)N;
+  const Geom& g = h->g;
+  const int wa_ = g.reg ? g.tha * 8 / P.ny : g.tla;
+  const int wb_ = g.reg ? g.thb * 8 / (P.nx / 2) : g.tlr;
+  const int wc_ = g.reg ? g.thc * 8 / P.ny : g.tlc;
   std::vector<WorkItem> wa, wb, wc;
   for (int f = 0; f < 3; ++f)
-    for (int t = 0; t < (int)ceil_div(nkd, h->g.tla); ++t) wa.push_back({0, t, f, 0});
-  for (int t = 0; t < (int)ceil_div(ny, h->g.tlr); ++t) wb.push_back({0, t, 0, 0});
-  for (int t = 0; t < (int)ceil_div(nkr, h->g.tlc); ++t) wc.push_back({0, t, 0, 0});
+    for (int t = 0; t < (int)ceil_div(P.nkd, wa_); ++t) wa.push_back({0, t, f, 0});
+  for (int t = 0; t < (int)ceil_div(P.ny, wb_); ++t) wb.push_back({0, t, 0, 0});
+  for (int t = 0; t < (int)ceil_div(P.nkr, wc_); ++t) wc.push_back({0, t, 0, 0});
   const size_t nw = wa.size() + wb.size() + wc.size();
   const size_t bytes = psz + nw * sizeof(WorkItem) + sizeof(void*);
-  // the staging buffer persists so that the asynchronous copies below can read it
   h->calc_host.resize(bytes);
   unsigned char* hp = h->calc_host.data();
-  memcpy(hp, desc.data(), psz);
+  memcpy(hp, &P, psz);
   memcpy(hp + psz, wa.data(), wa.size() * sizeof(WorkItem));
   memcpy(hp + psz + wa.size() * sizeof(WorkItem), wb.data(), wb.size() * sizeof(WorkItem));
   memcpy(hp + psz + (wa.size() + wb.size()) * sizeof(WorkItem), wc.data(), wc.size() * sizeof(WorkItem));
@@ -596,22 +662,14 @@ int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stre
   const void* dwb = base + psz + wa.size() * sizeof(WorkItem);
   const void* dwc = base + psz + (wa.size() + wb.size()) * sizeof(WorkItem);
   const void* din = base + psz + nw * sizeof(WorkItem);
-  if (f64) {
-    auto* P = (const VortProb<double>*)base;
-    k_vort_a<double><<<(int)wa.size(), h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)dwa, (int)wa.size(), h->g.tla,
-                                                                 (const double2* const*)din);
-    FF_LAUNCHED("k_vort_a");
-    k_vort_b<double><<<(int)wb.size(), h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)dwb, (int)wb.size(), h->g.tlr);
-    FF_LAUNCHED("k_vort_b");
-    return launch_c<double, EPI_N>(h, base, dwc, (int)wc.size(), (int)wc.size(), EpiScalars<double>{}, s);
-  }
-  auto* P = (const VortProb<float>*)base;
-  k_vort_a<float><<<(int)wa.size(), h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)dwa, (int)wa.size(), h->g.tla,
-                                                              (const float2* const*)din);
-  FF_LAUNCHED("k_vort_a");
-  k_vort_b<float><<<(int)wb.size(), h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)dwb, (int)wb.size(), h->g.tlr);
-  FF_LAUNCHED("k_vort_b");
-  return launch_c<float, EPI_N>(h, base, dwc, (int)wc.size(), (int)wc.size(), EpiScalars<float>{}, s);
+  if (int st = launch_a<T>(h, base, dwa, (int)wa.size(), (int)wa.size(), din, s)) return st;
+  if (int st = launch_b<T>(h, base, dwb, (int)wb.size(), (int)wb.size(), s)) return st;
+  return launch_c<T, EPI_N>(h, base, dwc, (int)wc.size(), (int)wc.size(), EpiScalars<T>{}, s);
 }
 
-}  // extern "C"
+extern "C" int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream) {
+  FF_CHECK_ARG(h && sol && N, "ff_vort_calcN: null argument");
+  FF_CHECK_ARG(prob >= 0 && prob < h->nprob, "ff_vort_calcN: problem index out of range");
+  auto s = (cudaStream_t)stream;
+  return h->prec == FF_F64 ? calcN_t<double>(h, prob, sol, N, s) : calcN_t<float>(h, prob, sol, N, s);
+}

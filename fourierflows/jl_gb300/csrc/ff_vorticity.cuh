@@ -23,6 +23,7 @@
 #pragma once
 
 #include "ff_fft.cuh"
+#include "ff_regfft.cuh"
 
 namespace ff {
 
@@ -290,6 +291,214 @@ __global__ void __launch_bounds__(512) k_vort_c(const VortProb<T>* __restrict__ 
         if (c < nkr) epilogue<T, EPI>(P, S, (int64_t)c + (int64_t)j * nkr, czero<T>());
       }
     }
+  }
+}
+
+// =======================================================================================
+// register-resident passes for power-of-two lengths (ff_regfft.cuh)
+// =======================================================================================
+// A CTA of nt threads (a power of two) holds nt*8 elements: tl = nt*8/N lines of length
+// N.  Columns map thread -> (t, ln) with the line fastest, so every load and store of a
+// warp touches tl consecutive columns of (32/tl) rows; rows map thread -> (ln, t).
+// Loads go straight from HBM to registers and results straight back; shared memory
+// holds only the exchanges between stages.
+
+template <typename T, int NY>
+__device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __restrict__ zh, int tile, int f,
+                                           cx<T>* smem) {
+  constexpr int PP = NY / 8;
+  const int tl = blockDim.x / PP;
+  const int ln = threadIdx.x & (tl - 1), t = threadIdx.x / tl;
+  const int c = tile * tl + ln;
+  const int nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb;
+  cx<T> v[1][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int j = t + q * PP;
+    cx<T> z = czero<T>();
+    if (c < nkd && (j < la || j >= lb)) {
+      const int64_t e = (int64_t)c + (int64_t)j * nkr;
+      const cx<T> s = zh[e];
+      if (f == 0) z = mul_i(scl(s, P.l[j] * P.invK[e]));
+      else if (f == 1) z = mul_mi(scl(s, P.kr[c] * P.invK[e]));
+      else z = s;
+    }
+    v[0][q] = z;
+  }
+  cx<T>* const buf[1] = {smem};
+  regfft<T, 1, NY, 1>(v, t, P.twy, buf, XCol{tl, ln});
+  if (c < nkd) {
+    cx<T>* Wf = P.W + (int64_t)f * nkd * P.ny;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Wf[c + (int64_t)(t + q * PP) * nkd] = v[0][q];
+  }
+}
+
+template <typename T, int H>
+__device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>* smem) {
+  constexpr int PP = H / 8;
+  constexpr int SH = sizeof(T) == 8 ? 3 : 4;
+  constexpr int STRIDE = H + (H >> SH) + 1;
+  const int rows = blockDim.x / PP;
+  const int ln = threadIdx.x / PP, t = threadIdx.x & (PP - 1);
+  const int j = tile * rows + ln;
+  const int ny = P.ny, nkd = P.nkd;
+  const int64_t fstride = (int64_t)nkd * ny;
+  cx<T> v[3][8];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    const cx<T>* src = P.W + f * fstride + (int64_t)j * nkd;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = t + q * PP;
+      cx<T> val = czero<T>();
+      if (j < ny) {
+        const cx<T> xk = k < nkd ? src[k] : czero<T>();
+        const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
+        val = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]), k);
+      }
+      v[f][q] = val;
+    }
+  }
+  const int bufsz = rows * STRIDE;
+  cx<T>* const buf3[3] = {smem, smem + bufsz, smem + 2 * bufsz};
+  const XRow xr{ln * STRIDE, SH};
+  regfft<T, 3, H, 1>(v, t, P.twx, buf3, xr);
+  // products u zeta and v zeta in physical space (packed real pairs), normalisation folded in
+  const T s2 = P.scale2;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const cx<T> z = v[2][q];
+    v[0][q] = mk<T>(v[0][q].x * z.x * s2, v[0][q].y * z.y * s2);
+    v[1][q] = mk<T>(v[1][q].x * z.x * s2, v[1][q].y * z.y * s2);
+  }
+  cx<T>(&p)[2][8] = *reinterpret_cast<cx<T>(*)[2][8]>(&v[0][0]);
+  regfft<T, 2, H, -1>(p, t, P.twx, buf3, xr);
+  // unpack X[k] = E + W O needs Z[H - k], held by another thread: one more exchange
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    buf3[0][xr(t + q * PP)] = p[0][q];
+    buf3[1][xr(t + q * PP)] = p[1][q];
+  }
+  __syncthreads();
+  if (j < ny) {
+    cx<T>* q0 = P.Q + (int64_t)j * nkd;
+    cx<T>* q1 = q0 + fstride;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = t + q * PP;
+      if (k >= nkd) continue;
+      cx<T> x0, x1, dummy;
+      if (k == 0) {
+        const cx<T> z0 = p[0][0], z1 = p[1][0];
+        x0 = mk<T>(z0.x + z0.y, T(0));
+        x1 = mk<T>(z1.x + z1.y, T(0));
+        if (nkd > H) {  // no dealiasing: the Nyquist column too
+          q0[H] = mk<T>(z0.x - z0.y, T(0));
+          q1[H] = mk<T>(z1.x - z1.y, T(0));
+        }
+      } else {
+        const cx<T> w = __ldg(&P.rtw[k]);
+        r2c_pair<T>(p[0][q], buf3[0][xr(H - k)], w, x0, dummy);
+        r2c_pair<T>(p[1][q], buf3[1][xr(H - k)], w, x1, dummy);
+      }
+      q0[k] = x0;
+      q1[k] = x1;
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int NY, int EPI>
+__device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalars<T>& S, int tile, cx<T>* smem) {
+  constexpr int PP = NY / 8;
+  const int tl = blockDim.x / PP;
+  const int ln = threadIdx.x & (tl - 1), t = threadIdx.x / tl;
+  const int c0 = tile * tl, c = c0 + ln;
+  const int nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb, ny = P.ny;
+  if (c0 < nkd) {
+    cx<T> v[2][8];
+    const int64_t fstride = (int64_t)nkd * ny;
+#pragma unroll
+    for (int f = 0; f < 2; ++f)
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        v[f][q] = c < nkd ? P.Q[f * fstride + c + (int64_t)(t + q * PP) * nkd] : czero<T>();
+    cx<T>* const buf2[2] = {smem, smem + (NY + NY / 8) * tl};
+    regfft<T, 2, NY, -1>(v, t, P.twy, buf2, XCol{tl, ln});
+    if (c < nkr) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int j = t + q * PP;
+        cx<T> N = czero<T>();
+        if (c < nkd && (j < la || j >= lb)) N = mul_mi(add(scl(v[0][q], P.kr[c]), scl(v[1][q], P.l[j])));
+        epilogue<T, EPI>(P, S, (int64_t)c + (int64_t)j * nkr, N);
+      }
+    }
+  } else if (c < nkr) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) epilogue<T, EPI>(P, S, (int64_t)c + (int64_t)(t + q * PP) * nkr, czero<T>());
+  }
+}
+
+#define FF_REG_CASES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
+#define FF_REG_CASES_B(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048)
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_vort_a_r(const VortProb<T>* __restrict__ probs,
+                                                  const WorkItem* __restrict__ work, int nwork,
+                                                  const cx<T>* const* __restrict__ inputs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    const cx<T>* zh = inputs[it.prob];
+    switch (P.ny) {
+#define FF_A_CASE(N) \
+  case N: vort_a_reg<T, N>(P, zh, it.tile, it.field, smem); break;
+      FF_REG_CASES(FF_A_CASE)
+#undef FF_A_CASE
+      default: break;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_vort_b_r(const VortProb<T>* __restrict__ probs,
+                                                  const WorkItem* __restrict__ work, int nwork) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    switch (P.nx / 2) {
+#define FF_B_CASE(N) \
+  case N: vort_b_reg<T, N>(P, it.tile, smem); break;
+      FF_REG_CASES_B(FF_B_CASE)
+#undef FF_B_CASE
+      default: break;
+    }
+  }
+}
+
+template <typename T, int EPI>
+__global__ void __launch_bounds__(512) k_vort_c_r(const VortProb<T>* __restrict__ probs,
+                                                  const WorkItem* __restrict__ work, int nwork, EpiScalars<T> S) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    switch (P.ny) {
+#define FF_C_CASE(N) \
+  case N: vort_c_reg<T, N, EPI>(P, S, it.tile, smem); break;
+      FF_REG_CASES(FF_C_CASE)
+#undef FF_C_CASE
+      default: break;
+    }
+    __syncthreads();
   }
 }
 

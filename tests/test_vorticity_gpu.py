@@ -53,6 +53,53 @@ def test_fused_steppers_vs_oracle_fp64(ff, cuda, stepper):
     assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
 
 
+@pytest.fixture(params=["register", "generic"])
+def kernel_path(request, monkeypatch):
+    """Run a test on the register-resident power-of-two kernels and on the generic ones."""
+    if request.param == "generic":
+        monkeypatch.setenv("FF_VORT_GENERIC", "1")
+    else:
+        monkeypatch.delenv("FF_VORT_GENERIC", raising=False)
+    return request.param
+
+
+@pytest.mark.parametrize("stepper", ["ETDRK4", "RK4", "FilteredLSRK54"])
+@pytest.mark.parametrize("n,ny", [(32, 32), (128, 64), (64, 256)])
+def test_fused_paths_vs_oracle(ff, cuda, kernel_path, stepper, n, ny):
+    prob, oprob = make_pair(ff, n, stepper, ny=ny)
+    ff.stepforward_(prob, 6)
+    fs = prob.timestepper._native(prob.eqn).fs
+    assert (fs.config()["radix_order"] == -1) == (kernel_path == "register")
+    orc.stepforward(oprob, 6)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
+
+
+def test_calcN_register_path(ff, cuda):
+    for n, ny in [(64, 64), (256, 128), (32, 512)]:
+        prob, oprob = make_pair(ff, n, "ETDRK4", ny=ny)
+        N = ff.zeros(ff.GPU(), np.complex128, (n // 2 + 1, ny))
+        ff.Vorticity.calcN_(N, prob.sol, 0.0, prob.clock, prob.vars, prob.params, prob.grid)
+        No = np.zeros_like(oprob.sol)
+        orc.vorticity_calcN(No, oprob.sol, 0.0, None, None, None, oprob.grid)
+        assert rel(ff.to_numpy(N), No) < 1e-13, (n, ny)
+
+
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_uneven_ensemble_vs_oracle(ff, cuda, T):
+    """An ensemble of different sizes and viscosities advanced in one launch per pass: every
+    member matches its own oracle run."""
+    spec = [(32, 1e-3, 5), (128, 3e-4, 6), (64, 1e-4, 7), (128, 1e-5, 8), (256, 2e-4, 9)]
+    ens = ff.Vorticity.Ensemble(spec, mu=1e-2, dt=2e-3, T=T)
+    ens.stepforward_(8)
+    tol = 1e-12 if T == np.float64 else 2e-5
+    for (n, nu, seed), m in zip(spec, ens.members):
+        z0 = ff.Vorticity.random_phase_vorticity(n, seed=seed)
+        op = orc.VorticityProblem(n, 2 * math.pi, nu, 1e-2, 2e-3, "ETDRK4")
+        op.sol[...] = orc.rfft(z0.astype(T).astype(np.float64))
+        orc.stepforward(op, 8)
+        assert rel(ff.to_numpy(m.sol).astype(np.complex128), op.sol) < tol, (n, nu)
+
+
 @pytest.mark.parametrize("stepper", ["ForwardEuler", "AB3", "FilteredAB3"])
 def test_generic_steppers_with_native_calcN(ff, cuda, stepper):
     """Steppers without a fused path call the native calcN! between native substeps."""
