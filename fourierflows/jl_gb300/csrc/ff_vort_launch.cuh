@@ -1,0 +1,39 @@
+// Launch helpers of the fused vorticity passes.  The kernels are instantiated per
+// precision in ff_vort_launch_f32.cu / ff_vort_launch_f64.cu (compiled in parallel);
+// the host logic in ff_vorticity.cu only sees these declarations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace ff {
+
+struct PassLaunch {
+  int grid, threads;
+  size_t smem;
+  int tile;   // generic path: tile width / rows per CTA
+  bool reg;   // register-resident power-of-two kernels
+};
+
+struct EpiArgs {  // precision-independent copy of EpiScalars
+  double c, b, dt;
+  int first, use_filter;
+};
+
+template <typename T>
+int vort_launch_a(const PassLaunch& L, const void* probs, const void* work, int nwork, const void* inputs,
+                  cudaStream_t s);
+template <typename T>
+int vort_launch_b(const PassLaunch& L, const void* probs, const void* work, int nwork, cudaStream_t s);
+// epi: one of the Epilogue values of ff_vorticity.cuh
+template <typename T>
+int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork, const EpiArgs& S,
+                  cudaStream_t s);
+
+// kernel entry points (for occupancy queries and shared-memory limits)
+template <typename T> const void* vort_kernel_a(bool reg);
+template <typename T> const void* vort_kernel_b(bool reg);
+template <typename T> const void* vort_kernel_c(bool reg, int epi);
+
+constexpr int kNumEpilogues = 10;
+
+}  // namespace ff

@@ -1,0 +1,6 @@
+// Fused vorticity kernels instantiated for FP32.
+#include "ff_vort_launch_impl.cuh"
+
+namespace ff {
+FF_INSTANTIATE_VORT_LAUNCH(float)
+}  // namespace ff

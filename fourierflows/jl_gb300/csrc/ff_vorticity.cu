@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "ff_plan.cuh"
+#include "ff_vort_launch.cuh"
 #include "ff_vorticity.cuh"
 
 using namespace ff;
@@ -285,56 +286,39 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   FF_CUDA(cudaMalloc(&h->d_inputs, sizeof(void*) * in.size()));
   FF_CUDA(cudaMemcpy(h->d_inputs, in.data(), sizeof(void*) * in.size(), cudaMemcpyHostToDevice));
   h->g = geom;
-  const void* ka = geom.reg ? (const void*)k_vort_a_r<T> : (const void*)k_vort_a<T>;
-  const void* kb = geom.reg ? (const void*)k_vort_b_r<T> : (const void*)k_vort_b<T>;
+  const void* ka = vort_kernel_a<T>(geom.reg);
+  const void* kb = vort_kernel_b<T>(geom.reg);
   if (int st = ensure_smem(ka, geom.sma)) return st;
   if (int st = ensure_smem(kb, geom.smb)) return st;
-#define FF_SMEM_C(E)                                                                                       \
-  if (int st = ensure_smem(geom.reg ? (const void*)k_vort_c_r<T, E> : (const void*)k_vort_c<T, E>, geom.smc)) \
-    return st;
-  FF_SMEM_C(EPI_N) FF_SMEM_C(EPI_ETD1) FF_SMEM_C(EPI_ETD2) FF_SMEM_C(EPI_ETD3) FF_SMEM_C(EPI_ETD4)
-  FF_SMEM_C(EPI_RK1) FF_SMEM_C(EPI_RK2) FF_SMEM_C(EPI_RK3) FF_SMEM_C(EPI_RK4) FF_SMEM_C(EPI_LS)
-#undef FF_SMEM_C
+  for (int e = 0; e < kNumEpilogues; ++e)
+    if (int st = ensure_smem(vort_kernel_c<T>(geom.reg, e), geom.smc)) return st;
   h->g.ga = grid_for<T>(ka, geom.tha, geom.sma, h->nwork_a);
   h->g.gb = grid_for<T>(kb, geom.thb, geom.smb, h->nwork_b);
-  h->g.gc = grid_for<T>(geom.reg ? (const void*)k_vort_c_r<T, EPI_ETD1> : (const void*)k_vort_c<T, EPI_ETD1>,
-                        geom.thc, geom.smc, h->nwork_c);
+  h->g.gc = grid_for<T>(vort_kernel_c<T>(geom.reg, EPI_ETD1), geom.thc, geom.smc, h->nwork_c);
   if (h->exec) { cudaGraphExecDestroy(h->exec); h->exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
   return FF_OK;
 }
 
-// launches of one pass over a descriptor array and work list (generic or register path)
+// launches of one pass over a descriptor array and work list (generic or register path);
+// the kernels themselves are instantiated in ff_vort_launch_f32.cu / _f64.cu
 template <typename T>
 int launch_a(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, const void* inputs,
              cudaStream_t s) {
-  const auto* P = (const VortProb<T>*)probs;
-  if (h->g.reg)
-    k_vort_a_r<T><<<grid, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)work, nwork, (const cx<T>* const*)inputs);
-  else
-    k_vort_a<T><<<grid, h->g.tha, h->g.sma, s>>>(P, (const WorkItem*)work, nwork, h->g.tla,
-                                                 (const cx<T>* const*)inputs);
-  FF_LAUNCHED("k_vort_a");
-  return FF_OK;
+  return vort_launch_a<T>(PassLaunch{grid, h->g.tha, h->g.sma, h->g.tla, h->g.reg}, probs, work, nwork, inputs, s);
 }
 
 template <typename T>
 int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, cudaStream_t s) {
-  const auto* P = (const VortProb<T>*)probs;
-  if (h->g.reg) k_vort_b_r<T><<<grid, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)work, nwork);
-  else k_vort_b<T><<<grid, h->g.thb, h->g.smb, s>>>(P, (const WorkItem*)work, nwork, h->g.tlr);
-  FF_LAUNCHED("k_vort_b");
-  return FF_OK;
+  return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg}, probs, work, nwork, s);
 }
 
 template <typename T, int EPI>
 int launch_c(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, EpiScalars<T> S,
              cudaStream_t s) {
-  const auto* P = (const VortProb<T>*)probs;
-  if (h->g.reg) k_vort_c_r<T, EPI><<<grid, h->g.thc, h->g.smc, s>>>(P, (const WorkItem*)work, nwork, S);
-  else k_vort_c<T, EPI><<<grid, h->g.thc, h->g.smc, s>>>(P, (const WorkItem*)work, nwork, h->g.tlc, S);
-  FF_LAUNCHED("k_vort_c");
-  return FF_OK;
+  const EpiArgs a{(double)S.c, (double)S.b, (double)S.dt, S.first, S.use_filter};
+  return vort_launch_c<T>(PassLaunch{grid, h->g.thc, h->g.smc, h->g.tlc, h->g.reg}, EPI, probs, work, nwork, a,
+                          s);
 }
 
 // one calcN! (passes A, B, C) with epilogue EPI on all problems; `inputs` = pass-A sources

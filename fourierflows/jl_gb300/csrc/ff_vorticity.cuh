@@ -317,7 +317,7 @@ __device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __
     const int j = t + q * PP;
     cx<T> z = czero<T>();
     if (c < nkd && (j < la || j >= lb)) {
-      const int64_t e = (int64_t)c + (int64_t)j * nkr;
+      const int e = c + j * nkr;
       const cx<T> s = zh[e];
       if (f == 0) z = mul_i(scl(s, P.l[j] * P.invK[e]));
       else if (f == 1) z = mul_mi(scl(s, P.kr[c] * P.invK[e]));
@@ -328,9 +328,9 @@ __device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __
   cx<T>* const buf[1] = {smem};
   regfft<T, 1, NY, 1>(v, t, P.twy, buf, XCol{tl, ln});
   if (c < nkd) {
-    cx<T>* Wf = P.W + (int64_t)f * nkd * P.ny;
+    cx<T>* Wf = P.W + f * nkd * P.ny + c;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) Wf[c + (int64_t)(t + q * PP) * nkd] = v[0][q];
+    for (int q = 0; q < 8; ++q) Wf[(t + q * PP) * nkd] = v[0][q];
   }
 }
 
@@ -343,11 +343,11 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   const int ln = threadIdx.x / PP, t = threadIdx.x & (PP - 1);
   const int j = tile * rows + ln;
   const int ny = P.ny, nkd = P.nkd;
-  const int64_t fstride = (int64_t)nkd * ny;
+  const int fstride = nkd * ny;
   cx<T> v[3][8];
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
-    const cx<T>* src = P.W + f * fstride + (int64_t)j * nkd;
+    const cx<T>* src = P.W + f * fstride + j * nkd;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = t + q * PP;
@@ -382,7 +382,7 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   }
   __syncthreads();
   if (j < ny) {
-    cx<T>* q0 = P.Q + (int64_t)j * nkd;
+    cx<T>* q0 = P.Q + j * nkd;
     cx<T>* q1 = q0 + fstride;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -418,12 +418,13 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
   const int nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb, ny = P.ny;
   if (c0 < nkd) {
     cx<T> v[2][8];
-    const int64_t fstride = (int64_t)nkd * ny;
+    const cx<T>* qsrc = P.Q + c;
+    const int fstride = nkd * ny;
 #pragma unroll
     for (int f = 0; f < 2; ++f)
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        v[f][q] = c < nkd ? P.Q[f * fstride + c + (int64_t)(t + q * PP) * nkd] : czero<T>();
+        v[f][q] = c < nkd ? qsrc[f * fstride + (t + q * PP) * nkd] : czero<T>();
     cx<T>* const buf2[2] = {smem, smem + (NY + NY / 8) * tl};
     regfft<T, 2, NY, -1>(v, t, P.twy, buf2, XCol{tl, ln});
     if (c < nkr) {
@@ -432,20 +433,47 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
         const int j = t + q * PP;
         cx<T> N = czero<T>();
         if (c < nkd && (j < la || j >= lb)) N = mul_mi(add(scl(v[0][q], P.kr[c]), scl(v[1][q], P.l[j])));
-        epilogue<T, EPI>(P, S, (int64_t)c + (int64_t)j * nkr, N);
+        epilogue<T, EPI>(P, S, c + j * nkr, N);
       }
     }
   } else if (c < nkr) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) epilogue<T, EPI>(P, S, (int64_t)c + (int64_t)(t + q * PP) * nkr, czero<T>());
+    for (int q = 0; q < 8; ++q) epilogue<T, EPI>(P, S, c + (t + q * PP) * nkr, czero<T>());
   }
 }
+
+// Register budgets of the register-path kernels: max threads per CTA and the minimum
+// number of resident CTAs per SM the compiler must fit
+#ifndef FF_LB_A_MIN_F32
+#define FF_LB_A_MIN_F32 2
+#endif
+#ifndef FF_LB_B_MIN_F32
+#define FF_LB_B_MIN_F32 1
+#endif
+#ifndef FF_LB_C_MIN_F32
+#define FF_LB_C_MIN_F32 1
+#endif
+#ifndef FF_LB_A_MIN_F64
+#define FF_LB_A_MIN_F64 2
+#endif
+#ifndef FF_LB_B_MIN_F64
+#define FF_LB_B_MIN_F64 1
+#endif
+#ifndef FF_LB_C_MIN_F64
+#define FF_LB_C_MIN_F64 1
+#endif
+template <typename T> struct RegBudget;  // minimum resident CTAs per SM by precision
+template <> struct RegBudget<float> { static constexpr int A = FF_LB_A_MIN_F32, B = FF_LB_B_MIN_F32, C = FF_LB_C_MIN_F32; };
+template <> struct RegBudget<double> { static constexpr int A = FF_LB_A_MIN_F64, B = FF_LB_B_MIN_F64, C = FF_LB_C_MIN_F64; };
+#define FF_LB_A 512, RegBudget<T>::A
+#define FF_LB_B 256, RegBudget<T>::B
+#define FF_LB_C 512, RegBudget<T>::C
 
 #define FF_REG_CASES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 #define FF_REG_CASES_B(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048)
 
 template <typename T>
-__global__ void __launch_bounds__(512) k_vort_a_r(const VortProb<T>* __restrict__ probs,
+__global__ void __launch_bounds__(FF_LB_A) k_vort_a_r(const VortProb<T>* __restrict__ probs,
                                                   const WorkItem* __restrict__ work, int nwork,
                                                   const cx<T>* const* __restrict__ inputs) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -466,7 +494,7 @@ __global__ void __launch_bounds__(512) k_vort_a_r(const VortProb<T>* __restrict_
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_vort_b_r(const VortProb<T>* __restrict__ probs,
+__global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restrict__ probs,
                                                   const WorkItem* __restrict__ work, int nwork) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
@@ -484,7 +512,7 @@ __global__ void __launch_bounds__(256) k_vort_b_r(const VortProb<T>* __restrict_
 }
 
 template <typename T, int EPI>
-__global__ void __launch_bounds__(512) k_vort_c_r(const VortProb<T>* __restrict__ probs,
+__global__ void __launch_bounds__(FF_LB_C) k_vort_c_r(const VortProb<T>* __restrict__ probs,
                                                   const WorkItem* __restrict__ work, int nwork, EpiScalars<T> S) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
