@@ -445,19 +445,19 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
 // Register budgets of the register-path kernels: max threads per CTA and the minimum
 // number of resident CTAs per SM the compiler must fit
 #ifndef FF_LB_A_MIN_F32
-#define FF_LB_A_MIN_F32 2
+#define FF_LB_A_MIN_F32 3
 #endif
 #ifndef FF_LB_B_MIN_F32
-#define FF_LB_B_MIN_F32 1
+#define FF_LB_B_MIN_F32 2
 #endif
 #ifndef FF_LB_C_MIN_F32
-#define FF_LB_C_MIN_F32 1
+#define FF_LB_C_MIN_F32 2
 #endif
 #ifndef FF_LB_A_MIN_F64
 #define FF_LB_A_MIN_F64 2
 #endif
 #ifndef FF_LB_B_MIN_F64
-#define FF_LB_B_MIN_F64 1
+#define FF_LB_B_MIN_F64 2
 #endif
 #ifndef FF_LB_C_MIN_F64
 #define FF_LB_C_MIN_F64 1
