@@ -387,7 +387,75 @@ def run_forms(torch, ff, a, hbm, peak_src):
     out["ensemble_uneven_384"] = {"value": 384 * 1e3 / msu, "unit": "problem-steps/s", "ms_per_step": msu,
                                   "grid_point_steps_per_s": gp * 1e3 / msu, "problems": 384,
                                   "sizes": "128x128^2 + 128x256^2 + 96x512^2 + 32x1024^2", "dtype": "f32"}
+    del ens
+    out["diffusion3d_64x128^3"] = diffusion3d_ensemble(torch, ff, a, hbm, peak_src, flush)
+    out["precision_2048"] = precision_2048(torch, ff)
     return out
+
+
+def precision_2048(torch, ff):
+    """FP32 state and transforms against the FP64 run of the same 2048^2 problem, for ETDRK4
+    and FilteredRK4 (order 4, innerK 0.65): relative L2 of zeta at steps 100 and 1000 and
+    the largest relative energy / enstrophy deviation over the series sampled every 100 steps."""
+    import numpy as np
+    n = 2048
+    z0 = ff.Vorticity.random_phase_vorticity(n, seed=SEED)
+    out = {}
+    for stepper, kw in (("ETDRK4", {}), ("FilteredRK4", {"order": 4, "innerK": 0.65})):
+        probs = {}
+        for T in (np.float64, np.float32):
+            p = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=NU, mu=MU, dt=DT, stepper=stepper, T=T, **kw)
+            ff.Vorticity.set_zeta_(p, z0)
+            probs[T] = p
+        p64, p32 = probs[np.float64], probs[np.float32]
+        res, eE, eZ, t32 = {}, 0.0, 0.0, 0.0
+        for chunk in range(10):
+            ff.stepforward_(p64, 100)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ff.stepforward_(p32, 100)
+            torch.cuda.synchronize()
+            t32 += time.perf_counter() - t0
+            E64, E32 = ff.Vorticity.energy(p64), ff.Vorticity.energy(p32)
+            Z64, Z32 = ff.Vorticity.enstrophy(p64), ff.Vorticity.enstrophy(p32)
+            eE, eZ = max(eE, abs(E32 - E64) / E64), max(eZ, abs(Z32 - Z64) / Z64)
+            if chunk in (0, 9):
+                s64 = ff.to_numpy(p64.sol)
+                s32 = ff.to_numpy(p32.sol).astype(np.complex128)
+                res[f"rel_l2_step{100 * (chunk + 1)}"] = float(np.linalg.norm(s32 - s64) / np.linalg.norm(s64))
+        res.update({"energy_max_rel_err": eE, "enstrophy_max_rel_err": eZ, "energy_final": E64,
+                    "fp32_steps_per_s": 1000 / t32, "finite": bool(np.isfinite(E64) and np.isfinite(E32))})
+        out[stepper] = res
+        del probs, p64, p32
+    return out
+
+
+def diffusion3d_ensemble(torch, ff, a, hbm, peak_src, flush):
+    """64 constant-kappa diffusion problems on ThreeDGrid 128^3 (kappa uniform in [1e-3, 1e-2],
+    Gaussian blobs), FP32 ETDRK4 dt = 2e-3, stacked so each substep is one native pass."""
+    import numpy as np
+    B, n = 64, 128
+    kappas = 1e-3 + 9e-3 * ff.Vorticity.uniform01(77, B)
+    ens = ff.Diffusion.Ensemble3D(kappas, n=n, dt=DT, T=np.float32)
+    ens.stepforward_(a.warmup)
+    steps = max(5, min(a.steps, 30))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for e0, e1 in ev:
+        flush.add_(1.0)
+        e0.record()
+        ens.stepforward_(1)
+        e1.record()
+    torch.cuda.synchronize()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / steps
+    C = (n // 2 + 1) * n * n * B * 8  # one complex state array
+    R = C // 2                         # one real coefficient array
+    # 2 x substep12 (3C + 2R), substep3 (4C + 2R), update (6C + 4R), 4 zero fills of N (4C)
+    byts = 20 * C + 10 * R
+    gbs = byts / (ms * 1e-3) / 1e9
+    return {"value": B * 1e3 / ms, "unit": "problem-steps/s", "ms_per_step": ms, "problems": B,
+            "grid_point_steps_per_s": ens.grid_points * 1e3 / ms, "dtype": "f32",
+            "algorithmic_bytes_per_step": byts, "achieved_gbs": gbs, "frac": gbs / hbm, "peak_source": peak_src,
+            "kernels_per_step": "4 N fills + ff_etdrk4_substep12 x2 + substep3 + update"}
 
 
 def profile_case(a):

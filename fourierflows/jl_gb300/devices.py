@@ -139,7 +139,12 @@ def device_array(dev, T=None, dim=None):
             elif T is not None:
                 a = a.astype(T)
             t = fortran_empty(a.shape, torch_dtype(a.dtype))
-            t.copy_(torch.from_numpy(np.ascontiguousarray(a)))
+            if a.ndim > 1 and a.flags.f_contiguous:
+                # same memory order on both sides: a plain copy, no host transpose
+                src = torch.from_numpy(a.T).permute(*reversed(range(a.ndim)))
+            else:
+                src = torch.from_numpy(np.ascontiguousarray(a))
+            t.copy_(src)
             return t
         return to_gpu
 

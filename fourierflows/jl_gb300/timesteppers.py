@@ -294,15 +294,23 @@ class ETDRK4TimeStepper(AbstractTimeStepper):
     """Exponential time differencing RK4 (Kassam & Trefethen 2005), src/timesteppers.jl:434-547."""
     _filtered = False
 
-    def __init__(self, equation, dt, dev=None, **kw):
+    def __init__(self, equation, dt, dev=None, coefficients="host", **kw):
+        """``coefficients="device"`` evaluates the contour means in FP64 on the GPU
+        (``ff_etdrk4_coefficients``) instead of on the host; meant for very large real L."""
         dev = dev if dev is not None else GPU()
         _require_gpu(dev)
         Tf = fltype(equation.T)
         dt = Tf(dt)
         eL, ehL = getexpLs(dt, equation)
-        z, a, b, g = getetdcoeffs(dt, equation.L)
         self.expLdt, self.exp_half_Ldt = _to_device_like(eL, equation, dev), _to_device_like(ehL, equation, dev)
-        self.zeta, self.alpha, self.beta, self.Gamma = (_to_device_like(c, equation, dev) for c in (z, a, b, g))
+        if coefficients == "device" and on_device(equation.L) and not equation.L.dtype.is_complex:
+            L = equation.L
+            self.zeta, self.alpha, self.beta, self.Gamma = (zeros(dev, Tf, tuple(L.shape)) for _ in range(4))
+            _lib.call("ff_etdrk4_coefficients", prec_of(L.dtype), L.numel(), ptr(L, "L"), float(dt), 32, 1.0,
+                      ptr(self.zeta), ptr(self.alpha), ptr(self.beta), ptr(self.Gamma), stream_handle())
+        else:
+            z, a, b, g = getetdcoeffs(dt, equation.L)
+            self.zeta, self.alpha, self.beta, self.Gamma = (_to_device_like(c, equation, dev) for c in (z, a, b, g))
         T, d = equation.T, equation.dims
         self.sol1, self.sol2, self.N1, self.N2, self.N3, self.N4 = (zeros(dev, T, d) for _ in range(6))
         self.filter = _setup_filter(equation, dev, kw) if self._filtered else None
