@@ -50,6 +50,7 @@ def args_():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-forms", action="store_true", help="skip the FP32 / batched / ensemble forms")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the differentiation form")
     p.add_argument("--profile-case", default="", help="run only a small case for ncu (fp64|fp32|batch)")
     return p.parse_args()
 
@@ -292,7 +293,8 @@ def our_arm(a):
     e2e = world * e2e_steps / (time.perf_counter() - t0)
     h2d = prob.sol.numel() * prob.sol.element_size()
 
-    forms = {} if a.no_forms else run_forms(torch, ff, a, hbm, peak_src)
+    # the precision / batching / differentiation forms are single-GPU measurements
+    forms = {} if (a.no_forms or world > 1) else run_forms(torch, ff, a, hbm, peak_src)
 
     cpu = None
     if rank == 0 and not a.no_cpu:
@@ -390,6 +392,8 @@ def run_forms(torch, ff, a, hbm, peak_src):
     del ens
     out["diffusion3d_64x128^3"] = diffusion3d_ensemble(torch, ff, a, hbm, peak_src, flush)
     out["precision_2048"] = precision_2048(torch, ff)
+    if not a.no_adjoint:
+        out["adjoint_512"] = adjoint_512(torch, ff)
     return out
 
 
@@ -399,12 +403,16 @@ def precision_2048(torch, ff):
     the largest relative energy / enstrophy deviation over the series sampled every 100 steps."""
     import numpy as np
     n = 2048
+    # dt = 2e-3 puts the kept modes past the advective stability limit at 2048^2
+    # (k_max u_max dt = 681 * 2.78 * 2e-3 = 3.8 > 2.83 for RK4 and ETDRK4: both precisions
+    # blow up); dt = 1e-3 keeps the CFL number of the 1024^2 configuration (1.9)
+    dt = 1e-3
     z0 = ff.Vorticity.random_phase_vorticity(n, seed=SEED)
-    out = {}
+    out = {"dt": dt}
     for stepper, kw in (("ETDRK4", {}), ("FilteredRK4", {"order": 4, "innerK": 0.65})):
         probs = {}
         for T in (np.float64, np.float32):
-            p = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=NU, mu=MU, dt=DT, stepper=stepper, T=T, **kw)
+            p = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=NU, mu=MU, dt=dt, stepper=stepper, T=T, **kw)
             ff.Vorticity.set_zeta_(p, z0)
             probs[T] = p
         p64, p32 = probs[np.float64], probs[np.float32]
@@ -456,6 +464,67 @@ def diffusion3d_ensemble(torch, ff, a, hbm, peak_src, flush):
             "grid_point_steps_per_s": ens.grid_points * 1e3 / ms, "dtype": "f32",
             "algorithmic_bytes_per_step": byts, "achieved_gbs": gbs, "frac": gbs / hbm, "peak_source": peak_src,
             "kernels_per_step": "4 N fills + ff_etdrk4_substep12 x2 + substep3 + update"}
+
+
+def adjoint_512(torch, ff, ndir=8, nsteps=2000):
+    """Discrete adjoint of 512^2 ETDRK4 (dt 2e-3, 2000 steps, checkpoint every 50): FP32
+    forward and adjoint with FP64 gradient reductions; loss = mean((zeta_T - zeta_target)^2)
+    + enstrophy(zeta_T); directional derivatives along seeded random directions against
+    FP64 central differences with h in {1e-3, 1e-4, 1e-5}, and d/dnu likewise."""
+    import numpy as np
+    n, nu, mu, dt = 512, NU, MU, DT
+    z0 = ff.Vorticity.random_phase_vorticity(n, seed=SEED + 5)
+    zt = ff.Vorticity.random_phase_vorticity(n, seed=SEED + 6)
+    dev = ff.device_array(ff.GPU())
+    out = {"grid": "512^2", "steps": nsteps, "checkpoint_every": 50, "directions": ndir}
+    res = {}
+    for T, name in ((np.float32, "fp32"), (np.float64, "fp64")):
+        p = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=nu, mu=mu, dt=dt, stepper="ETDRK4", T=T)
+        adj = ff.Adjoint.VorticityAdjoint(p, checkpoint_every=50)
+        tgt = ff.rfft(dev(zt.astype(T)))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L, gz, dnu = adj.gradient(z0, tgt, nsteps)
+        torch.cuda.synchronize()
+        res[name] = {"loss": L, "grad": ff.to_numpy(gz).astype(np.float64), "dnu": dnu,
+                     "seconds": time.perf_counter() - t0}
+        del adj, p
+    p64 = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=nu, mu=mu, dt=dt, stepper="ETDRK4", T=np.float64)
+    a64 = ff.Adjoint.VorticityAdjoint(p64)
+    tgt64 = ff.rfft(dev(zt))
+
+    def loss_at(z, prob=p64, ad=a64):
+        ff.Vorticity.set_zeta_(prob, z)
+        ff.stepforward_(prob, nsteps)
+        return ad.loss(tgt64)
+
+    rng = np.random.default_rng(SEED + 7)
+    worst = {name: {h: 0.0 for h in (1e-3, 1e-4, 1e-5)} for name in res}
+    for _ in range(ndir):
+        d = rng.standard_normal((n, n))
+        for h in (1e-3, 1e-4, 1e-5):
+            fd = (loss_at(z0 + h * d) - loss_at(z0 - h * d)) / (2 * h)
+            for name in res:
+                dl = float(np.sum(res[name]["grad"] * d))
+                worst[name][h] = max(worst[name][h], abs(dl - fd) / abs(fd))
+    nu_rel = {}
+    for h in (1e-7, 1e-8):
+        vals = []
+        for sgn in (1, -1):
+            pn = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=nu + sgn * h, mu=mu, dt=dt, stepper="ETDRK4",
+                                      T=np.float64)
+            an = ff.Adjoint.VorticityAdjoint(pn)
+            vals.append(loss_at(z0, pn, an))
+            del an, pn
+        fd = (vals[0] - vals[1]) / (2 * h)
+        nu_rel[f"h={h:g}"] = {name: abs(res[name]["dnu"] - fd) / abs(fd) for name in res}
+    for name in res:
+        out[name] = {"loss": res[name]["loss"], "d_loss_d_nu": res[name]["dnu"],
+                     "gradient_seconds": res[name]["seconds"],
+                     "adjoint_steps_per_s": nsteps / res[name]["seconds"],
+                     "max_rel_err_vs_fp64_fd": {f"h={h:g}": v for h, v in worst[name].items()}}
+    out["nu_rel_err_vs_fp64_fd"] = nu_rel
+    return out
 
 
 def profile_case(a):

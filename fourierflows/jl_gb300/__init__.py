@@ -21,6 +21,8 @@ from .utils import innereltype, jacobian, jacobianh, on_grid, parsevalsum, parse
 from .diagnostics import AbstractDiagnostic, Diagnostic, extend_, increment_, update_
 from . import diffusion as Diffusion
 from . import vorticity as Vorticity
+from . import adjoint as Adjoint
+from .adjoint import rrule_stepforward
 
 __version__ = "0.1.0"
 

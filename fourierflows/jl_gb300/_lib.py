@@ -78,7 +78,17 @@ SIGNATURES = {
     "ff_etdrk4_coefficients": [i32, i64, vp, f64, i32, f64, vp, vp, vp, vp, vp],
     "ff_fp64_peak": [C.POINTER(f64), vp],
     "ff_parsevalsum2_noalloc": [i32, vp, i64, i64, i32, f64, vp, vp],
+    "ff_vadj_create": [i32, i64, i64, i64, i64, i64, vp, vp, vp, C.POINTER(vp)],
+    "ff_vadj_destroy": [vp],
+    "ff_vadj_apply": [vp, vp, vp, vp, vp],
+    "ff_vort_adj_nu_terms": [vp, vp, f64, vp, vp],
 }
+
+
+class ff_adj_nu(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in
+                ("lam", "lam_a", "lam_b", "lam_c", "s", "a", "n1", "n2", "n3", "n4", "dE", "dE2", "dZ", "dA", "dB",
+                 "dG")]
 
 FF_STEP_ETDRK4, FF_STEP_RK4, FF_STEP_LSRK54 = 0, 1, 2
 

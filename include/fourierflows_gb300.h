@@ -242,6 +242,34 @@ int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stre
  * ETDRK4 and RK4 writes only the stepper's intermediate buffers. */
 int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]);
 
+/* ---- discrete adjoint of the 2D vorticity term and of an ETDRK4 step -------------------- */
+/* No counterpart in FourierFlows.jl (whose gradients would come from an AD system through
+ * `stepforward!`); these serve a ChainRulesCore `rrule` for stepforward! over the fused
+ * vorticity step.  The state is the stored half spectrum read as a real vector of its
+ * real and imaginary parts (inner product sum Re(conj(a) b)). */
+typedef struct ff_vadj ff_vadj;
+
+int ff_vadj_create(int prec, int64_t nx, int64_t ny, int64_t nkd, int64_t la, int64_t lb, const void* kr,
+                   const void* l, const void* invKrsq, ff_vadj** out);
+int ff_vadj_destroy(ff_vadj* h);
+
+/* out = J(s)^T lam: the transpose of the linearisation of N at state s applied to lam
+ * (nkr*ny complex each; out may alias lam). */
+int ff_vadj_apply(ff_vadj* h, const void* s, const void* lam, void* out, void* stream);
+
+/* Arrays of one adjoint ETDRK4 step: the adjoints of the new state and of sol1 (a), of
+ * the first sol2 (b) and of the second sol2 (c); the step's s, a and N1..N4; and the
+ * derivatives with respect to the viscosity of expLdt, exp_half_Ldt, zeta, alpha, beta and
+ * Gamma (real arrays). */
+typedef struct {
+  const void *lam, *lam_a, *lam_b, *lam_c, *s, *a, *n1, *n2, *n3, *n4;
+  const void *dE, *dE2, *dZ, *dA, *dB, *dG;
+} ff_adj_nu;
+
+/* *dev_acc += scale * d(step)/d(nu) contracted with the adjoints, accumulated in FP64 on
+ * the device (no host synchronisation). */
+int ff_vort_adj_nu_terms(ff_vadj* h, const ff_adj_nu* args, double scale, double* dev_acc, void* stream);
+
 /* Launch geometry: cfg = {tile A, tile C, rows B, radix order, threads A, B, C, graph}. */
 int ff_vort_config(const ff_vort* h, int32_t cfg[8]);
 int ff_vort_set_config(ff_vort* h, int tla, int tlc, int tlr, int radix_variant);

@@ -607,6 +607,45 @@ def vorticity_calcN(N, sol, t, clock, vars, params, g):
     N[...] = dealias(out, g).astype(N.dtype)
 
 
+def vorticity_bilinear(ah, bh, g):
+    """B(a, b) = -dealias(d/dx(u_a zeta_b) + d/dy(v_a zeta_b)), velocity from a, vorticity
+    from b, both inputs dealiased; vorticity_calcN is B(s, s)."""
+    ad = dealias(np.array(ah, copy=True), g)
+    bd = dealias(np.array(bh, copy=True), g)
+    psih = -ad * g.invKrsq
+    u = irfft(-1j * g.l * psih, g.nx)
+    v = irfft(1j * g.kr * psih, g.nx)
+    z = irfft(bd, g.nx)
+    return dealias(-(1j * g.kr * rfft(u * z) + 1j * g.l * rfft(v * z)), g)
+
+
+def vorticity_calcN_tangent(sh, dsh, g):
+    """Forward-mode tangent of the vorticity term at s along ds: B(ds, s) + B(s, ds)."""
+    return vorticity_bilinear(dsh, sh, g) + vorticity_bilinear(sh, dsh, g)
+
+
+def etdrk4_vorticity_tangent_step(s, ds, ts, g):
+    """One ETDRK4 step (src/timesteppers.jl:501-547) of the vorticity problem and its
+    tangent along ds: returns (s', ds')."""
+    def N(x):
+        out = np.zeros_like(x)
+        vorticity_calcN(out, x, 0.0, None, None, None, g)
+        return out
+
+    E, E2, Z, al, be, ga = ts.expLdt, ts.exp_half_Ldt, ts.zeta, ts.alpha, ts.beta, ts.Gamma
+    N1 = N(s)
+    dN1 = vorticity_calcN_tangent(s, ds, g)
+    a, da = E2 * s + Z * N1, E2 * ds + Z * dN1
+    N2, dN2 = N(a), vorticity_calcN_tangent(a, da, g)
+    b, db = E2 * s + Z * N2, E2 * ds + Z * dN2
+    N3, dN3 = N(b), vorticity_calcN_tangent(b, db, g)
+    c, dc = E2 * a + Z * (2 * N3 - N1), E2 * da + Z * (2 * dN3 - dN1)
+    N4, dN4 = N(c), vorticity_calcN_tangent(c, dc, g)
+    s2 = E * s + al * N1 + 2 * be * (N2 + N3) + ga * N4
+    ds2 = E * ds + al * dN1 + 2 * be * (dN2 + dN3) + ga * dN4
+    return s2, ds2
+
+
 def VorticityProblem(n, L, nu, mu, dt, stepper="ETDRK4", T=np.float64, aliased_fraction=1 / 3, **kw):
     g = TwoDGrid(n, L, T=T, aliased_fraction=aliased_fraction)
     Lop = (-nu * g.Krsq - mu).astype(T)

@@ -209,3 +209,19 @@ def test_show_strings_grid_values():
     g3 = orc.ThreeDGrid(6, 2 * math.pi, 8, 4 * math.pi, 10, 3.0)
     assert repr(float(g3.y[-1])) == "4.71238898038469" and repr(float(g3.z[0])) == "-1.5"
     assert repr(float(g3.z[-1])) == "1.2"
+
+
+def test_vorticity_tangent_matches_central_differences():
+    """The oracle's forward-mode tangent of an ETDRK4 step agrees with central differences
+    of the oracle step (the reference CPU path the GPU adjoint is checked against)."""
+    g_prob = orc.VorticityProblem(32, 2 * math.pi, 1e-3, 1e-2, 2e-3, "ETDRK4")
+    ts, g = g_prob.timestepper, g_prob.grid
+    rng = np.random.default_rng(2)
+    s = orc.dealias(orc.rfft(rng.standard_normal((32, 32))), g)
+    ds = orc.rfft(rng.standard_normal((32, 32)))
+    _, tan = orc.etdrk4_vorticity_tangent_step(s, ds, ts, g)
+    h = 1e-6
+    sp, _ = orc.etdrk4_vorticity_tangent_step(s + h * ds, ds, ts, g)
+    sm, _ = orc.etdrk4_vorticity_tangent_step(s - h * ds, ds, ts, g)
+    fd = (sp - sm) / (2 * h)
+    assert np.linalg.norm(fd - tan) / np.linalg.norm(tan) < 1e-8

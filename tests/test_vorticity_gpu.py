@@ -165,6 +165,16 @@ def test_full_size_1024_fp64_short_horizon(ff, cuda):
     assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
 
 
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_precision_size_2048_two_steps(ff, cuda, T):
+    """The 2048^2 grid of the precision form: two ETDRK4 steps against the FP64 oracle."""
+    prob, oprob = make_pair(ff, 2048, "ETDRK4", T=T, nu=1e-4, mu=1e-2, dt=1e-3, seed=31)
+    ff.stepforward_(prob, 2)
+    orc.stepforward(oprob, 2)
+    tol = 1e-12 if T == np.float64 else 2e-6
+    assert rel(ff.to_numpy(prob.sol).astype(np.complex128), oprob.sol) < tol
+
+
 def test_full_size_properties_1024(ff, cuda):
     """Size-independent properties at 1024^2: the state stays 2/3-dealiased, energy decays
     monotonically under viscosity + drag, and FP32 tracks FP64 on the GPU."""
