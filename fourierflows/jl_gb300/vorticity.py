@@ -202,12 +202,14 @@ class VorticityCalcN:
     """Native N = -J(psi, zeta) with 2/3 dealiasing; see the module docstring."""
     __name__ = "calcN!"
 
-    def __init__(self):
-        self._handles = {}
-
     def _handle(self, grid, sol):
-        key = (id(grid), str(sol.dtype))
-        fs = self._handles.get(key)
+        # the handle lives on the grid (same lifetime as the arrays it points to), one per
+        # precision; never keyed by id(), which a later grid can reuse
+        if tuple(sol.shape) != (grid.nkr, grid.ny):
+            raise ValueError(f"calcN!: state of size {tuple(sol.shape)} on a {grid.nx} x {grid.ny} grid")
+        handles = grid.__dict__.setdefault("_vort_calcN_handles", {})
+        key = str(sol.dtype)
+        fs = handles.get(key)
         if fs is None:
             q = _vort_problem_struct(grid, sol)
             scratch = zeros(grid.device, cxtype(grid.T), (grid.nkr, grid.ny))
@@ -220,7 +222,7 @@ class VorticityCalcN:
             q.sol = ptr(scratch).value
             fs = FusedStepper("ETDRK4", False, 0.0, prec_of(sol.dtype), [q],
                               [scratch, grid.kr, grid.l, grid.invKrsq])
-            self._handles[key] = fs
+            handles[key] = fs
         return fs
 
     def __call__(self, N, sol, t, clock, vars, params, grid):
