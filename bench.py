@@ -52,6 +52,7 @@ def args_():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiation form")
     p.add_argument("--profile-case", default="", help="run only a small case for ncu (fp64|fp32|batch)")
+    p.add_argument("--tiles", default="", help="profile case: tile_a,tile_c,rows_b (default: the library's)")
     return p.parse_args()
 
 
@@ -369,13 +370,15 @@ def run_forms(torch, ff, a, hbm, peak_src):
     dom = max(passes, key=lambda k: passes[k][0])
     ach = passes[dom][1] / (passes[dom][0] * 1e-3) / 1e9
     step_ach = 32 * bts["step"] / (msb * 1e-3) / 1e9
+    step_sv = 32 * survey_step_bytes(N, 4) / (msb * 1e-3) / 1e9
     out["fp32_batched_1024x32"] = {
         "value": 32 * 1e3 / msb, "unit": "problem-steps/s (1024^2 ETDRK4)", "ms_per_step": msb,
         "tiles": ens.fs.config(), "l2": "working set 1.8 GB > L2; flushed between steps",
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                      "kernel": f"k_vort_{dom.lower()} (pass {dom})", "peak_source": peak_src,
                      "pass_ms": {"A": tA, "B": tB, "C": tC}},
-        "step_algorithmic_gbs": step_ach, "step_frac": step_ach / hbm}
+        "step_algorithmic_gbs": step_ach, "step_frac": step_ach / hbm,
+        "step_survey_gbs": step_sv, "step_survey_frac": step_sv / hbm}
     del ens, saved
     # the uneven ensemble: 128 x 128^2, 128 x 256^2, 96 x 512^2, 32 x 1024^2, nu log-uniform
     u = ff.Vorticity.uniform01(99, 384)
@@ -487,7 +490,8 @@ def adjoint_512(torch, ff, ndir=8, nsteps=2000):
         L, gz, dnu = adj.gradient(z0, tgt, nsteps)
         torch.cuda.synchronize()
         res[name] = {"loss": L, "grad": ff.to_numpy(gz).astype(np.float64), "dnu": dnu,
-                     "seconds": time.perf_counter() - t0}
+                     "seconds": time.perf_counter() - t0,
+                     "final": ff.to_numpy(p.sol).astype(np.complex128)}
         del adj, p
     p64 = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=nu, mu=mu, dt=dt, stepper="ETDRK4", T=np.float64)
     a64 = ff.Adjoint.VorticityAdjoint(p64)
@@ -524,6 +528,12 @@ def adjoint_512(torch, ff, ndir=8, nsteps=2000):
                      "adjoint_steps_per_s": nsteps / res[name]["seconds"],
                      "max_rel_err_vs_fp64_fd": {f"h={h:g}": v for h, v in worst[name].items()}}
     out["nu_rel_err_vs_fp64_fd"] = nu_rel
+    # what bounds the FP32 figures: the FP32 forward map itself drifts from the FP64 one
+    g32, g64 = res["fp32"]["grad"], res["fp64"]["grad"]
+    f32, f64 = res["fp32"]["final"], res["fp64"]["final"]
+    out["fp32_vs_fp64"] = {"grad_rel_l2": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
+                           "final_zeta_rel_l2": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
+                           "loss_rel": abs(res["fp32"]["loss"] - res["fp64"]["loss"]) / abs(res["fp64"]["loss"])}
     return out
 
 
@@ -537,11 +547,13 @@ def profile_case(a):
     torch.cuda.set_device(0)
     if a.profile_case == "batch":
         ens = ff.Vorticity.Ensemble([(N, NU, SEED + i) for i in range(4)], mu=MU, dt=DT, T=np.float32)
-        ens.fs.advance(a.steps)
+        fs = ens.fs
     else:
         T = np.float64 if a.profile_case == "fp64" else np.float32
         prob, fs = make_problem(ff, T)
-        fs.advance(a.steps)
+    if a.tiles:
+        fs.set_config(*[int(x) for x in a.tiles.split(",")])
+    fs.advance(a.steps)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": a.profile_case, "steps": a.steps}))
 

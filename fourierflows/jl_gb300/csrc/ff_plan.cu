@@ -85,6 +85,7 @@ int upload_table(const std::vector<double>& t, int prec, void** dev) {
 
 int ensure_smem(const void* func, size_t bytes) {
   if (bytes <= 48 * 1024) return FF_OK;
+  FF_CHECK_ARG(bytes <= 227 * 1024, "shared memory request of %zu bytes exceeds 227 KB", bytes);
   static std::mutex mu;
   static std::set<std::pair<const void*, int>> done;
   int dev = 0;

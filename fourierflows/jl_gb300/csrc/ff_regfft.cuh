@@ -35,23 +35,27 @@ struct XRow {
   __device__ __forceinline__ int operator()(int p) const { return base + p + (p >> sh); }
 };
 
+// twiddles W_N^(k r TWS), r = 1..7, of a radix-8 stage of span NS > 1 (k = t mod NS): the
+// only stages with twiddles, since a smaller radix only ever opens a transform
+template <typename T, int N, int NS>
+__device__ __forceinline__ void stage_twiddles(int t, const cx<T>* __restrict__ tw, cx<T> (&w)[8]) {
+  constexpr int TWS = N / (NS * 8);
+  const int k = t & (NS - 1);
+#pragma unroll
+  for (int r = 1; r < 8; ++r) w[r] = __ldg(&tw[k * r * TWS]);
+}
+
+// one stage of span NS with its twiddles w already in registers; the next stage's
+// twiddles are loaded before the exchange so that their latency hides behind it
 template <typename T, int F, int N, int DIR, int NS, class X>
 __device__ __forceinline__ void regfft_from(cx<T> (&v)[F][8], int t, const cx<T>* __restrict__ tw,
-                                            cx<T>* const* buf, X x) {
+                                            cx<T>* const* buf, X x, const cx<T> (&w)[8]) {
   constexpr int L = ilog2c(N);
   constexpr int R = (NS == 1 && (L % 3) != 0) ? (1 << (L % 3)) : 8;
   constexpr int M = 8 / R;
   constexpr int P = N / 8;
-  constexpr int TWS = N / (NS * R);
 #pragma unroll
   for (int m = 0; m < M; ++m) {
-    const int j = t + m * P;
-    const int k = j & (NS - 1);
-    cx<T> w[R];
-    if (NS > 1) {
-#pragma unroll
-      for (int r = 1; r < R; ++r) w[r] = __ldg(&tw[k * r * TWS]);
-    }
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       cx<T> u[R];
@@ -67,6 +71,8 @@ __device__ __forceinline__ void regfft_from(cx<T> (&v)[F][8], int t, const cx<T>
     }
   }
   if constexpr (NS * R < N) {
+    cx<T> wn[8];
+    stage_twiddles<T, N, NS * R>(t, tw, wn);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int m = q % M, r = q / M;
@@ -82,7 +88,7 @@ __device__ __forceinline__ void regfft_from(cx<T> (&v)[F][8], int t, const cx<T>
 #pragma unroll
       for (int f = 0; f < F; ++f) v[f][q] = buf[f][x(t + q * P)];
     __syncthreads();
-    regfft_from<T, F, N, DIR, NS * R, X>(v, t, tw, buf, x);
+    regfft_from<T, F, N, DIR, NS * R, X>(v, t, tw, buf, x, wn);
   }
 }
 
@@ -90,7 +96,8 @@ __device__ __forceinline__ void regfft_from(cx<T> (&v)[F][8], int t, const cx<T>
 template <typename T, int F, int N, int DIR, class X>
 __device__ __forceinline__ void regfft(cx<T> (&v)[F][8], int t, const cx<T>* __restrict__ tw, cx<T>* const* buf,
                                        X x) {
-  regfft_from<T, F, N, DIR, 1, X>(v, t, tw, buf, x);
+  const cx<T> none[8] = {};
+  regfft_from<T, F, N, DIR, 1, X>(v, t, tw, buf, x, none);
 }
 
 }  // namespace ff

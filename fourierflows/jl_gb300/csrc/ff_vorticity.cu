@@ -18,6 +18,7 @@ struct Geom {
                                    // (register path: lines per CTA of the largest problem)
   int tha = 0, thb = 0, thc = 0;   // threads per CTA
   size_t sma = 0, smb = 0, smc = 0;
+  int stage_b = 0;                 // register path: elements per pipeline stage of pass B
   int ga = 0, gb = 0, gc = 0;      // grid sizes
   int radix_variant = 0;           // generic path: 0 radix-8 first, 1 radix-4 first, 2 small radix first
   bool reg = false;                // register-resident power-of-two kernels
@@ -79,6 +80,7 @@ struct ff_vort {
   std::vector<void*> tables;    // twiddle tables
   void* d_W = nullptr;
   void* d_Q = nullptr;
+  int* d_status = nullptr;     // FF_DEV_* flags set by the kernels
   Geom g;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
@@ -98,6 +100,12 @@ bool reg_capable(const ff_vort* h) {
   for (const auto& q : h->host)
     if (!regfft_ok((int)q.ny) || !regfft_ok((int)(q.nx / 2)) || q.nx / 2 > 2048) return false;
   return true;
+}
+
+// row pitch of W and Q in elements: rows start on 16-byte boundaries for the bulk copies
+static int64_t wq_pitch(int64_t nkd, size_t es) {
+  const int64_t m = 16 / (int64_t)es;
+  return (nkd + m - 1) / m * m;
 }
 
 template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, int tlr) {
@@ -122,16 +130,34 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
   g.tla = g.tha * 8 / ny;
   g.tlc = g.thc * 8 / ny;
   g.tlr = g.thb * 8 / hx;
-  g.sma = 9 * (size_t)g.tha * es;
+  g.sma = 9 * (size_t)AFields<T>::value * g.tha * es;
   g.smc = 2 * 9 * (size_t)g.thc * es;
-  size_t smb = 0;
+  // pass B, after 128 bytes of barriers: two stages, each holding a row block of W
+  // (3 x rows x nkp), and the exchanges (3 x rows x padded stride), which either reuse
+  // the stage (FF_B_OVERLAY) or follow the two stages
   const int sh = f64 ? 3 : 4;
-  for (const auto& q : h->host) {
-    const int H = (int)(q.nx / 2);
-    const size_t rows = (size_t)g.thb * 8 / H;
-    smb = std::max(smb, 3 * rows * (size_t)(H + (H >> sh) + 1) * es);
+  for (;;) {  // fewer rows per CTA until the stages fit the 227 KB of a CTA
+    size_t stage = 0, exch = 0;
+    for (const auto& q : h->host) {
+      const int H = (int)(q.nx / 2);
+      const size_t rows = (size_t)g.thb * 8 / H;
+      exch = std::max(exch, 3 * rows * (size_t)(H + (H >> sh) + 1));
+      stage = std::max(stage, 3 * rows * (size_t)wq_pitch(q.nkd, es));
+    }
+    const size_t m = 16 / es;
+    if (FF_B_OVERLAY) {
+      stage = std::max(stage, exch);
+      stage = (stage + m - 1) / m * m;
+      g.smb = 128 + 2 * stage * es;
+    } else {
+      stage = (stage + m - 1) / m * m;
+      g.smb = 128 + (2 * stage + exch) * es;
+    }
+    g.stage_b = (int)stage;
+    if (g.smb <= 227 * 1024 || g.thb <= std::max(32, hx / 8)) break;
+    g.thb /= 2;
+    g.tlr = g.thb * 8 / hx;
   }
-  g.smb = smb;
   return g;
 }
 
@@ -180,6 +206,7 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
     P.ny = (int)q.ny;
     P.nkr = (int)(q.nx / 2 + 1);
     P.nkd = (int)q.nkd;
+    P.nkp = (int)wq_pitch(q.nkd, elem<T>());
     P.la = (int)q.la;
     P.lb = (int)q.lb;
     const double s = 1.0 / ((double)q.nx * (double)q.ny);
@@ -208,7 +235,7 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
     P.invK = (const T*)q.invKrsq;
     P.W = (cx<T>*)h->d_W + woff * 3;
     P.Q = (cx<T>*)h->d_Q + woff * 2;
-    woff += (int64_t)P.nkd * P.ny;
+    woff += (int64_t)P.nkp * P.ny;
     P.sol = (cx<T>*)q.sol;
     P.filter = (const T*)q.filter;
     if (h->stepper == FF_STEP_ETDRK4) {
@@ -241,7 +268,8 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
     const int wb_ = geom.reg ? geom.thb * 8 / (P.nx / 2) : geom.tlr;
     const int wc_ = geom.reg ? geom.thc * 8 / P.ny : geom.tlc;
     const int ta = (int)ceil_div(P.nkd, wa_);
-    for (int f = 0; f < 3; ++f)
+    const int afields = geom.reg && AFields<T>::value == 3 ? 1 : 3;  // work items per tile
+    for (int f = 0; f < afields; ++f)
       for (int tt = 0; tt < ta; ++tt) wa.push_back({(int)i, tt, f, 0});
     const int tb = (int)ceil_div(P.ny, wb_);
     for (int tt = 0; tt < tb; ++tt) wb.push_back({(int)i, tt, 0, 0});
@@ -310,7 +338,8 @@ int launch_a(const ff_vort* h, const void* probs, const void* work, int nwork, i
 
 template <typename T>
 int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, cudaStream_t s) {
-  return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg}, probs, work, nwork, s);
+  return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg, h->g.stage_b, h->d_status}, probs,
+                          work, nwork, s);
 }
 
 template <typename T, int EPI>
@@ -406,7 +435,7 @@ void destroy(ff_vort* h) {
   if (h->graph) cudaGraphDestroy(h->graph);
   for (void* p : h->tables) cudaFree(p);
   for (void* p : {h->d_probs, h->d_calc_prob, h->d_work_a, h->d_work_b, h->d_work_c, h->d_calc_work, h->d_inputs,
-                  h->d_calc_input, h->d_W, h->d_Q})
+                  h->d_calc_input, h->d_W, h->d_Q, (void*)h->d_status})
     if (p) cudaFree(p);
   delete h;
 }
@@ -456,12 +485,14 @@ int ff_vort_create(int prec, int stepper, int filtered, double dt, int64_t nprob
     h->max_nx = std::max<int>(h->max_nx, (int)q.nx);
     h->max_ny = std::max<int>(h->max_ny, (int)q.ny);
     h->max_nkd = std::max<int>(h->max_nkd, (int)q.nkd);
-    wsize += q.nkd * q.ny;
+    wsize += wq_pitch(q.nkd, prec == FF_F64 ? 16 : 8) * q.ny;
   }
   const size_t es = prec == FF_F64 ? 16 : 8;
   int st = FF_OK;
   cudaError_t e = cudaMalloc(&h->d_W, 3 * wsize * es);
   if (e == cudaSuccess) e = cudaMalloc(&h->d_Q, 2 * wsize * es);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(int));
   if (e != cudaSuccess) st = cuda_status(e, "ff_vort_create: workspace");
   if (st == FF_OK) {
     const char* nog = getenv("FF_NO_GRAPH");
@@ -478,6 +509,16 @@ int ff_vort_create(int prec, int stepper, int filtered, double dt, int64_t nprob
 
 int ff_vort_destroy(ff_vort* h) {
   destroy(h);
+  return FF_OK;
+}
+
+int ff_vort_status(ff_vort* h, int32_t* flags) {
+  FF_CHECK_ARG(h && flags, "ff_vort_status: null argument");
+  int v = 0;
+  FF_CUDA(cudaDeviceSynchronize());
+  FF_CUDA(cudaMemcpy(&v, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  FF_CUDA(cudaMemset(h->d_status, 0, sizeof(int)));
+  *flags = v;
   return FF_OK;
 }
 
@@ -618,7 +659,8 @@ template <typename T> int calcN_t(ff_vort* h, int64_t prob, const void* sol, voi
   const int wb_ = g.reg ? g.thb * 8 / (P.nx / 2) : g.tlr;
   const int wc_ = g.reg ? g.thc * 8 / P.ny : g.tlc;
   std::vector<WorkItem> wa, wb, wc;
-  for (int f = 0; f < 3; ++f)
+  const int afields = g.reg && AFields<T>::value == 3 ? 1 : 3;
+  for (int f = 0; f < afields; ++f)
     for (int t = 0; t < (int)ceil_div(P.nkd, wa_); ++t) wa.push_back({0, t, f, 0});
   for (int t = 0; t < (int)ceil_div(P.ny, wb_); ++t) wb.push_back({0, t, 0, 0});
   for (int t = 0; t < (int)ceil_div(P.nkr, wc_); ++t) wc.push_back({0, t, 0, 0});

@@ -24,6 +24,21 @@
 
 #include "ff_fft.cuh"
 #include "ff_regfft.cuh"
+#include "ff_tma.cuh"
+
+// Pass B shared memory: two pipeline stages of input rows; the exchanges either reuse
+// the stage just read (1, one extra barrier per item) or have their own region (0)
+#ifndef FF_B_OVERLAY
+#define FF_B_OVERLAY 1
+#endif
+// Register pass A: fields per work item, 3 (u, v, zeta of a column tile together) or 1
+// (one work item per field: fewer registers, for FP64)
+#ifndef FF_A_FIELDS_F32
+#define FF_A_FIELDS_F32 3
+#endif
+#ifndef FF_A_FIELDS_F64
+#define FF_A_FIELDS_F64 1
+#endif
 
 namespace ff {
 
@@ -43,6 +58,7 @@ enum Epilogue {
 template <typename T> struct VortProb {
   int nx, ny, nkr, nkd;  // nkd: kept kr columns [0, nkd)
   int la, lb;            // aliased l rows [la, lb)
+  int nkp, pad0;         // row pitch of W and Q: nkd rounded up to 16 bytes
   T scale2;              // 1 / (nx ny)^2, applied to each physical product
   LinePlan Px, Py;       // length nx/2 and ny
   const cx<T>* twx;
@@ -51,8 +67,8 @@ template <typename T> struct VortProb {
   const T* kr;           // nkr
   const T* l;            // ny
   const T* invK;         // nkr * ny, 1/K^2 with the mean mode 0
-  cx<T>* W;              // 3 * nkd * ny
-  cx<T>* Q;              // 2 * nkd * ny
+  cx<T>* W;              // 3 * nkp * ny
+  cx<T>* Q;              // 2 * nkp * ny
   // stepper state (nkr * ny each)
   cx<T>* sol;
   cx<T>* s1;
@@ -114,10 +130,10 @@ __global__ void __launch_bounds__(512) k_vort_a(const VortProb<T>* __restrict__ 
     }
     __syncthreads();
     const cx<T>* R = fft_lines<T, 1>(A, B, P.twy, P.Py, tl, ad);
-    cx<T>* Wf = P.W + (int64_t)f * nkd * ny;
+    cx<T>* Wf = P.W + (int64_t)f * P.nkp * ny;
     for (int idx = threadIdx.x; idx < tl * ny; idx += blockDim.x) {
       const int ln = idx % tl, j = idx / tl, c = c0 + ln;
-      if (c < nkd) Wf[c + (int64_t)j * nkd] = R[ad(ln, j)];
+      if (c < nkd) Wf[c + (int64_t)j * P.nkp] = R[ad(ln, j)];
     }
     __syncthreads();
   }
@@ -139,7 +155,7 @@ __global__ void __launch_bounds__(512) k_vort_b(const VortProb<T>* __restrict__ 
     cx<T>* b0 = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* b[4] = {b0, b0 + bufsz, b0 + 2 * bufsz, b0 + 3 * bufsz};
     const int row0 = it.tile * tlr;
-    const int64_t fstride = (int64_t)nkd * ny;
+    const int64_t fstride = (int64_t)P.nkp * ny;
     // gather the three y-transformed fields and pack them for the C2R transforms
     for (int idx = threadIdx.x; idx < 3 * tlr * h; idx += blockDim.x) {
       const int f = idx / (tlr * h);
@@ -148,7 +164,7 @@ __global__ void __launch_bounds__(512) k_vort_b(const VortProb<T>* __restrict__ 
       const int j = row0 + ln;
       cx<T> v = czero<T>();
       if (j < ny) {
-        const cx<T>* src = P.W + f * fstride + (int64_t)j * nkd;
+        const cx<T>* src = P.W + f * fstride + (int64_t)j * P.nkp;
         const cx<T> xk = k < nkd ? src[k] : czero<T>();
         const cx<T> xh = (h - k) < nkd ? src[h - k] : czero<T>();
         v = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]), k);
@@ -190,8 +206,8 @@ __global__ void __launch_bounds__(512) k_vort_b(const VortProb<T>* __restrict__ 
         r2c_pair<T>(q0[ad(ln, k)], q0[ad(ln, h - k)], w, x0, dummy);
         r2c_pair<T>(q1[ad(ln, k)], q1[ad(ln, h - k)], w, x1, dummy);
       }
-      P.Q[(int64_t)j * nkd + k] = x0;
-      P.Q[fstride + (int64_t)j * nkd + k] = x1;
+      P.Q[(int64_t)j * P.nkp + k] = x0;
+      P.Q[fstride + (int64_t)j * P.nkp + k] = x1;
     }
     __syncthreads();
   }
@@ -264,11 +280,11 @@ __global__ void __launch_bounds__(512) k_vort_c(const VortProb<T>* __restrict__ 
       const AddrTile ad{nl};
       cx<T>* A = reinterpret_cast<cx<T>*>(smem_raw);
       cx<T>* B = A + nl * ny;
-      const int64_t fstride = (int64_t)nkd * ny;
+      const int64_t fstride = (int64_t)P.nkp * ny;
       for (int idx = threadIdx.x; idx < nl * ny; idx += blockDim.x) {
         const int ln = idx % nl, j = idx / nl;
         const int f = ln / tl, c = c0 + (ln - f * tl);
-        A[ad(ln, j)] = c < nkd ? P.Q[f * fstride + c + (int64_t)j * nkd] : czero<T>();
+        A[ad(ln, j)] = c < nkd ? P.Q[f * fstride + c + (int64_t)j * P.nkp] : czero<T>();
       }
       __syncthreads();
       const cx<T>* R = fft_lines<T, -1>(A, B, P.twy, P.Py, nl, ad);
@@ -303,6 +319,46 @@ __global__ void __launch_bounds__(512) k_vort_c(const VortProb<T>* __restrict__ 
 // Loads go straight from HBM to registers and results straight back; shared memory
 // holds only the exchanges between stages.
 
+// All three fields of a column tile in one work item: zeta_hat, 1/K^2 and l are read
+// once, and the three inverse transforms share twiddles, exchanges and barriers.
+template <typename T, int NY>
+__device__ __forceinline__ void vort_a_reg3(const VortProb<T>& P, const cx<T>* __restrict__ zh, int tile,
+                                            cx<T>* smem) {
+  constexpr int PP = NY / 8;
+  const int tl = blockDim.x / PP;
+  const int ln = threadIdx.x & (tl - 1), t = threadIdx.x / tl;
+  const int c = tile * tl + ln;
+  const int nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb;
+  const T kc = c < nkd ? P.kr[c] : T(0);
+  cx<T> v[3][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int j = t + q * PP;
+    cx<T> s = czero<T>();
+    T ik = T(0), lj = T(0);
+    if (c < nkd && (j < la || j >= lb)) {
+      const int e = c + j * nkr;
+      s = zh[e];
+      ik = P.invK[e];
+      lj = P.l[j];
+    }
+    v[0][q] = mul_i(scl(s, lj * ik));   // u_hat = i l zeta_hat / K^2
+    v[1][q] = mul_mi(scl(s, kc * ik));  // v_hat = -i kr zeta_hat / K^2
+    v[2][q] = s;
+  }
+  const int bsz = (NY + NY / 8) * tl;
+  cx<T>* const buf[3] = {smem, smem + bsz, smem + 2 * bsz};
+  regfft<T, 3, NY, 1>(v, t, P.twy, buf, XCol{tl, ln});
+  if (c < nkd) {
+    const int fs = P.nkp * P.ny;
+    cx<T>* Wc = P.W + c;
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) Wc[f * fs + (t + q * PP) * P.nkp] = v[f][q];
+  }
+}
+
 template <typename T, int NY>
 __device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __restrict__ zh, int tile, int f,
                                            cx<T>* smem) {
@@ -328,26 +384,31 @@ __device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __
   cx<T>* const buf[1] = {smem};
   regfft<T, 1, NY, 1>(v, t, P.twy, buf, XCol{tl, ln});
   if (c < nkd) {
-    cx<T>* Wf = P.W + f * nkd * P.ny + c;
+    cx<T>* Wf = P.W + f * P.nkp * P.ny + c;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) Wf[(t + q * PP) * nkd] = v[0][q];
+    for (int q = 0; q < 8; ++q) Wf[(t + q * PP) * P.nkp] = v[0][q];
   }
 }
 
+// The row block of W (3 fields x rows x nkp) sits in shared memory at `in` (a bulk copy,
+// see k_vort_b_r); the exchanges use `ex`, which with FF_B_OVERLAY is the same memory,
+// reused once every thread holds its inputs.  `ok`: this thread's wait for the copy
+// completed.  With the overlay, returns false, with nothing written, when any thread's
+// wait ran out (the barrier that guards the reuse carries that vote).
 template <typename T, int H>
-__device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>* smem) {
+__device__ __forceinline__ bool vort_b_reg(const VortProb<T>& P, int tile, const cx<T>* in, cx<T>* ex, bool ok) {
   constexpr int PP = H / 8;
   constexpr int SH = sizeof(T) == 8 ? 3 : 4;
   constexpr int STRIDE = H + (H >> SH) + 1;
   const int rows = blockDim.x / PP;
   const int ln = threadIdx.x / PP, t = threadIdx.x & (PP - 1);
   const int j = tile * rows + ln;
-  const int ny = P.ny, nkd = P.nkd;
-  const int fstride = nkd * ny;
+  const int ny = P.ny, nkd = P.nkd, nkp = P.nkp;
+  const int fstride = nkp * ny;
   cx<T> v[3][8];
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
-    const cx<T>* src = P.W + f * fstride + j * nkd;
+    const cx<T>* src = in + (f * rows + ln) * nkp;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = t + q * PP;
@@ -360,8 +421,9 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
       v[f][q] = val;
     }
   }
+  if (FF_B_OVERLAY && __syncthreads_or(!ok)) return false;
   const int bufsz = rows * STRIDE;
-  cx<T>* const buf3[3] = {smem, smem + bufsz, smem + 2 * bufsz};
+  cx<T>* const buf3[3] = {ex, ex + bufsz, ex + 2 * bufsz};
   const XRow xr{ln * STRIDE, SH};
   regfft<T, 3, H, 1>(v, t, P.twx, buf3, xr);
   // products u zeta and v zeta in physical space (packed real pairs), normalisation folded in
@@ -382,7 +444,7 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   }
   __syncthreads();
   if (j < ny) {
-    cx<T>* q0 = P.Q + j * nkd;
+    cx<T>* q0 = P.Q + j * P.nkp;
     cx<T>* q1 = q0 + fstride;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -406,7 +468,7 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
       q1[k] = x1;
     }
   }
-  __syncthreads();
+  return true;
 }
 
 template <typename T, int NY, int EPI>
@@ -419,12 +481,12 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
   if (c0 < nkd) {
     cx<T> v[2][8];
     const cx<T>* qsrc = P.Q + c;
-    const int fstride = nkd * ny;
+    const int fstride = P.nkp * ny;
 #pragma unroll
     for (int f = 0; f < 2; ++f)
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        v[f][q] = c < nkd ? qsrc[f * fstride + (t + q * PP) * nkd] : czero<T>();
+        v[f][q] = c < nkd ? qsrc[f * fstride + (t + q * PP) * P.nkp] : czero<T>();
     cx<T>* const buf2[2] = {smem, smem + (NY + NY / 8) * tl};
     regfft<T, 2, NY, -1>(v, t, P.twy, buf2, XCol{tl, ln});
     if (c < nkr) {
@@ -445,7 +507,7 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
 // Register budgets of the register-path kernels: max threads per CTA and the minimum
 // number of resident CTAs per SM the compiler must fit
 #ifndef FF_LB_A_MIN_F32
-#define FF_LB_A_MIN_F32 3
+#define FF_LB_A_MIN_F32 (FF_A_FIELDS_F32 == 3 ? 1 : 3)
 #endif
 #ifndef FF_LB_B_MIN_F32
 #define FF_LB_B_MIN_F32 2
@@ -454,7 +516,7 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
 #define FF_LB_C_MIN_F32 2
 #endif
 #ifndef FF_LB_A_MIN_F64
-#define FF_LB_A_MIN_F64 2
+#define FF_LB_A_MIN_F64 (FF_A_FIELDS_F64 == 3 ? 1 : 2)
 #endif
 #ifndef FF_LB_B_MIN_F64
 #define FF_LB_B_MIN_F64 2
@@ -462,12 +524,27 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
 #ifndef FF_LB_C_MIN_F64
 #define FF_LB_C_MIN_F64 1
 #endif
+// the final substeps (ETDRK4 / RK4 updates) read four state arrays and up to five
+// coefficient arrays in the epilogue: their own budget
+#ifndef FF_LB_C4_MIN_F32
+#define FF_LB_C4_MIN_F32 FF_LB_C_MIN_F32
+#endif
+#ifndef FF_LB_C4_MIN_F64
+#define FF_LB_C4_MIN_F64 FF_LB_C_MIN_F64
+#endif
+template <typename T> struct AFields;
+template <> struct AFields<float> { static constexpr int value = FF_A_FIELDS_F32; };
+template <> struct AFields<double> { static constexpr int value = FF_A_FIELDS_F64; };
 template <typename T> struct RegBudget;  // minimum resident CTAs per SM by precision
-template <> struct RegBudget<float> { static constexpr int A = FF_LB_A_MIN_F32, B = FF_LB_B_MIN_F32, C = FF_LB_C_MIN_F32; };
-template <> struct RegBudget<double> { static constexpr int A = FF_LB_A_MIN_F64, B = FF_LB_B_MIN_F64, C = FF_LB_C_MIN_F64; };
+template <> struct RegBudget<float> {
+  static constexpr int A = FF_LB_A_MIN_F32, B = FF_LB_B_MIN_F32, C = FF_LB_C_MIN_F32, C4 = FF_LB_C4_MIN_F32;
+};
+template <> struct RegBudget<double> {
+  static constexpr int A = FF_LB_A_MIN_F64, B = FF_LB_B_MIN_F64, C = FF_LB_C_MIN_F64, C4 = FF_LB_C4_MIN_F64;
+};
 #define FF_LB_A 512, RegBudget<T>::A
 #define FF_LB_B 256, RegBudget<T>::B
-#define FF_LB_C 512, RegBudget<T>::C
+#define FF_LB_C 512, ((EPI == EPI_ETD4 || EPI == EPI_RK4) ? RegBudget<T>::C4 : RegBudget<T>::C)
 
 #define FF_REG_CASES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 #define FF_REG_CASES_B(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048)
@@ -484,7 +561,10 @@ __global__ void __launch_bounds__(FF_LB_A) k_vort_a_r(const VortProb<T>* __restr
     const cx<T>* zh = inputs[it.prob];
     switch (P.ny) {
 #define FF_A_CASE(N) \
-  case N: vort_a_reg<T, N>(P, zh, it.tile, it.field, smem); break;
+  case N:                                                 \
+    if (AFields<T>::value == 3) vort_a_reg3<T, N>(P, zh, it.tile, smem); \
+    else vort_a_reg<T, N>(P, zh, it.tile, it.field, smem); \
+    break;
       FF_REG_CASES(FF_A_CASE)
 #undef FF_A_CASE
       default: break;
@@ -493,21 +573,75 @@ __global__ void __launch_bounds__(FF_LB_A) k_vort_a_r(const VortProb<T>* __restr
   }
 }
 
+// thread 0: arm `bar` and copy the three field-row blocks of item `it` into `stage`
+template <typename T>
+__device__ __forceinline__ void issue_rows_b(const VortProb<T>& P, const WorkItem& it, cx<T>* stage, uint64_t* bar) {
+  const int rows = blockDim.x * 8 / (P.nx / 2), j0 = it.tile * rows;
+  const int nr = min(rows, P.ny - j0);
+  const uint32_t bytes = (uint32_t)(nr * P.nkp) * (uint32_t)sizeof(cx<T>);
+  mbar_arrive_expect_tx(bar, 3 * bytes);
+  const int fstride = P.nkp * P.ny;
+#pragma unroll
+  for (int f = 0; f < 3; ++f) bulk_copy_g2s(stage + f * rows * P.nkp, P.W + f * fstride + j0 * P.nkp, bytes, bar);
+}
+
+// Pass B, persistent over row blocks with a two-stage pipeline: while one stage is
+// transformed (its input read, then reused for the exchanges) the bulk copy of the next
+// item's rows lands in the other.  stage: elements per stage (a multiple of 16 bytes).
 template <typename T>
 __global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restrict__ probs,
-                                                  const WorkItem* __restrict__ work, int nwork) {
+                                                  const WorkItem* __restrict__ work, int nwork, int stage,
+                                                  int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-    const WorkItem it = work[w];
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(smem_raw);
+  cx<T>* const st0 = reinterpret_cast<cx<T>*>(smem_raw + 128);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int nit = ((int)blockIdx.x < nwork) ? (nwork - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  if (threadIdx.x == 0 && nit > 0) issue_rows_b(probs[work[blockIdx.x].prob], work[blockIdx.x], st0, &bar[0]);
+  for (int i = 0; i < nit; ++i) {
+    const int s = i & 1;
+    if (threadIdx.x == 0 && i + 1 < nit) {
+      const WorkItem nxt = work[blockIdx.x + (i + 1) * gridDim.x];
+      issue_rows_b(probs[nxt.prob], nxt, st0 + (s ^ 1) * stage, &bar[s ^ 1]);
+    }
+    const bool ok = mbar_wait(&bar[s], (i >> 1) & 1);
+    const WorkItem it = work[blockIdx.x + i * gridDim.x];
     const VortProb<T>& P = probs[it.prob];
+    bool done = false;
     switch (P.nx / 2) {
 #define FF_B_CASE(N) \
-  case N: vort_b_reg<T, N>(P, it.tile, smem); break;
+  case N: done = vort_b_reg<T, N>(P, it.tile, st0 + s * stage, FF_B_OVERLAY ? st0 + s * stage : st0 + 2 * stage, ok); \
+    break;
       FF_REG_CASES_B(FF_B_CASE)
 #undef FF_B_CASE
-      default: break;
+      default: done = !FF_B_OVERLAY || !__syncthreads_or(!ok); break;
     }
+    if (!FF_B_OVERLAY && !ok) atomicOr(status, FF_DEV_WAIT_TIMEOUT);  // results invalid, flagged
+    if (!done) {
+      // a wait ran out: record it, let the copies in flight land (bounded) and stop
+      if (threadIdx.x == 0) {
+        atomicOr(status, FF_DEV_WAIT_TIMEOUT);
+        mbar_wait(&bar[s], (i >> 1) & 1);
+        if (i + 1 < nit) mbar_wait(&bar[s ^ 1], ((i + 1) >> 1) & 1);
+      }
+      return;
+    }
+    // this stage's shared memory is rewritten by a bulk copy two items on: with the
+    // overlay it also took generic-proxy writes (the exchanges), ordered before that
+    // copy by a proxy fence; otherwise it was only read, which the barrier orders
+    if (FF_B_OVERLAY) fence_proxy_async_smem();
+    __syncthreads();
+  }
+  // no copy may land after the CTA exits: the last phase of each barrier (returns at
+  // once when, as normally, it completed)
+  if (threadIdx.x == 0 && nit > 0) {
+    mbar_wait(&bar[(nit - 1) & 1], ((nit - 1) >> 1) & 1);
+    if (nit > 1) mbar_wait(&bar[nit & 1], ((nit - 2) >> 1) & 1);
   }
 }
 

@@ -116,6 +116,12 @@ class FusedStepper:
     def calcN(self, N, sol, prob=0, stream=None):
         _lib.call("ff_vort_calcN", self._h, int(prob), ptr(sol, "sol"), ptr(N, "N"), stream_handle(stream))
 
+    def status(self):
+        """Device status flags since the last call (0: every bounded wait completed)."""
+        flags = C.c_int32()
+        _lib.call("ff_vort_status", self._h, C.byref(flags))
+        return flags.value
+
     def profile(self, reps=10, stream=None):
         """Average device ms of passes A, B, C (CUDA events inside the library)."""
         ms = (C.c_double * 3)()
@@ -384,18 +390,25 @@ def random_phase_vorticity(nx, ny=None, Lx=2 * math.pi, Ly=None, seed=1234, k0=6
 class EnsembleMember:
     """State, stepper buffers and coefficients of one ensemble problem (device arrays)."""
 
-    def __init__(self, grid, nu, mu, dt, stepper, T):
-        from .timesteppers import getetdcoeffs
+    def __init__(self, grid, nu, mu, dt, stepper, T, like=None):
         self.grid, self.nu, self.mu = grid, nu, mu
         Tf = np.dtype(T).type
         Ct = cxtype(T)
         shape = (grid.nkr, grid.ny)
         dev = grid.device
-        L = (-nu * grid.Krsq_host.astype(np.float64) - mu).astype(Tf)
         self.sol = zeros(dev, Ct, shape)
+        self.kind = stepper.replace("Filtered", "")
+        nbuf = {"ETDRK4": 5, "RK4": 4, "LSRK54": 1}.get(self.kind)
+        if nbuf is None:
+            raise ValueError(f"the ensemble path supports ETDRK4, RK4 and LSRK54 (got {stepper})")
+        self.bufs = [zeros(dev, Ct, shape) for _ in range(nbuf)]
+        if like is not None:
+            # same grid, nu, mu, dt and stepper: the read-only operator arrays are shared
+            self.L, self.coefs, self.filter = like.L, like.coefs, like.filter
+            return
+        L = (-nu * grid.Krsq_host.astype(np.float64) - mu).astype(Tf)
         up = device_array(dev)
         self.L = up(L)
-        self.kind = stepper.replace("Filtered", "")
         if self.kind == "ETDRK4":
             dtT = Tf(dt)
             dtL = (dtT * L).astype(Tf)
@@ -405,15 +418,8 @@ class EnsembleMember:
             _lib.call("ff_etdrk4_coefficients", prec_of(self.L.dtype), self.L.numel(), ptr(self.L), float(dtT), 32,
                       1.0, ptr(zab[0]), ptr(zab[1]), ptr(zab[2]), ptr(zab[3]), stream_handle())
             self.coefs += zab
-            self.bufs = [zeros(dev, Ct, shape) for _ in range(5)]
-        elif self.kind == "RK4":
-            self.coefs = [self.L]
-            self.bufs = [zeros(dev, Ct, shape) for _ in range(4)]
-        elif self.kind == "LSRK54":
-            self.coefs = [self.L]
-            self.bufs = [zeros(dev, Ct, shape)]
         else:
-            raise ValueError(f"the ensemble path supports ETDRK4, RK4 and LSRK54 (got {stepper})")
+            self.coefs = [self.L]
         self.filter = None
         if stepper.startswith("Filtered"):
             from .domains import makefilter_host
@@ -424,7 +430,8 @@ class Ensemble:
     """Independent 2D vorticity problems of (possibly) different sizes advanced together:
     every substep is three persistent launches over all members and a step is one CUDA
     graph replay.  ``members`` are (n, nu, seed) triples; grids of equal size share their
-    wavenumber arrays.  ``value`` counters are problem-steps."""
+    wavenumber arrays, and members of equal size and viscosity share their operator and
+    coefficient arrays (read-only).  ``value`` counters are problem-steps."""
 
     def __init__(self, members, mu=1e-2, dt=2e-3, stepper="ETDRK4", T=np.float32, Lx=2 * math.pi, E0=0.5,
                  k0=6.0, dev=None):
@@ -434,12 +441,15 @@ class Ensemble:
         self.grids = {}
         self.members = []
         structs, keep = [], []
+        shared = {}
         for (n, nu, seed) in members:
             g = self.grids.get(n)
             if g is None:
                 g = TwoDGrid(dev, nx=n, Lx=Lx, T=T)
                 self.grids[n] = g
-            m = EnsembleMember(g, nu, mu, dt, stepper, T)
+            key = (n, float(nu))
+            m = EnsembleMember(g, nu, mu, dt, stepper, T, like=shared.get(key))
+            shared.setdefault(key, m)
             z0 = random_phase_vorticity(n, seed=seed, k0=k0, E0=E0)
             zd = device_array(dev)(z0.astype(self.T))
             mul_(m.sol, g.rfftplan, zd)

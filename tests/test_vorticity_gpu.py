@@ -98,6 +98,8 @@ def test_uneven_ensemble_vs_oracle(ff, cuda, T):
         op.sol[...] = orc.rfft(z0.astype(T).astype(np.float64))
         orc.stepforward(op, 8)
         assert rel(ff.to_numpy(m.sol).astype(np.complex128), op.sol) < tol, (n, nu)
+    # every bounded wait of the pipelined row pass completed
+    assert ens.fs.status() == 0
 
 
 @pytest.mark.parametrize("stepper", ["ForwardEuler", "AB3", "FilteredAB3"])
