@@ -75,7 +75,6 @@ SIGNATURES = {
     "ff_vort_set_config": [vp, i32, i32, i32, i32],
     "ff_vort_autotune": [vp, i32, vp, C.POINTER(f64)],
     "ff_vort_profile": [vp, i32, vp, C.POINTER(f64)],
-    "ff_vort_status": [vp, C.POINTER(C.c_int32)],
     "ff_etdrk4_coefficients": [i32, i64, vp, f64, i32, f64, vp, vp, vp, vp, vp],
     "ff_fp64_peak": [C.POINTER(f64), vp],
     "ff_parsevalsum2_noalloc": [i32, vp, i64, i64, i32, f64, vp, vp],

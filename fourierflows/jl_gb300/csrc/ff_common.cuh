@@ -55,6 +55,19 @@ FF_CX_OPS(double2, double)
 template <typename T> __device__ __forceinline__ cx<T> czero() { return mk<T>(T(0), T(0)); }
 
 // ---------------------------------------------------------------------------------------
+// L2 prefetch hints (no register result, no completion to wait for)
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// every 128-byte line of a contiguous span, spread over the threads of the CTA
+template <typename E> __device__ __forceinline__ void prefetch_lines(const E* p, int n, int lane, int lanes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(127);
+  const uintptr_t e = reinterpret_cast<uintptr_t>(p + n);
+  for (uintptr_t x = a + (uintptr_t)lane * 128; x < e; x += (uintptr_t)lanes * 128)
+    prefetch_l2(reinterpret_cast<const void*>(x));
+}
+
+// ---------------------------------------------------------------------------------------
 // errors
 // ---------------------------------------------------------------------------------------
 void set_error(const char* fmt, ...);

@@ -12,8 +12,6 @@ struct PassLaunch {
   size_t smem;
   int tile;   // generic path: tile width / rows per CTA
   bool reg;   // register-resident power-of-two kernels
-  int stage = 0;           // pass B, register path: elements per pipeline stage
-  int* status = nullptr;   // pass B, register path: device status word
 };
 
 struct EpiArgs {  // precision-independent copy of EpiScalars

@@ -33,7 +33,7 @@ int vort_launch_a(const PassLaunch& L, const void* probs, const void* work, int 
 template <typename T>
 int vort_launch_b(const PassLaunch& L, const void* probs, const void* work, int nwork, cudaStream_t s) {
   const auto* P = (const VortProb<T>*)probs;
-  if (L.reg) k_vort_b_r<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.stage, L.status);
+  if (L.reg) k_vort_b_r<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork);
   else k_vort_b<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.tile);
   FF_LAUNCHED("k_vort_b");
   return FF_OK;

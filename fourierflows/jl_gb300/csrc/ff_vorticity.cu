@@ -18,7 +18,6 @@ struct Geom {
                                    // (register path: lines per CTA of the largest problem)
   int tha = 0, thb = 0, thc = 0;   // threads per CTA
   size_t sma = 0, smb = 0, smc = 0;
-  int stage_b = 0;                 // register path: elements per pipeline stage of pass B
   int ga = 0, gb = 0, gc = 0;      // grid sizes
   int radix_variant = 0;           // generic path: 0 radix-8 first, 1 radix-4 first, 2 small radix first
   bool reg = false;                // register-resident power-of-two kernels
@@ -80,7 +79,6 @@ struct ff_vort {
   std::vector<void*> tables;    // twiddle tables
   void* d_W = nullptr;
   void* d_Q = nullptr;
-  int* d_status = nullptr;     // FF_DEV_* flags set by the kernels
   Geom g;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
@@ -132,32 +130,14 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
   g.tlr = g.thb * 8 / hx;
   g.sma = 9 * (size_t)AFields<T>::value * g.tha * es;
   g.smc = 2 * 9 * (size_t)g.thc * es;
-  // pass B, after 128 bytes of barriers: two stages, each holding a row block of W
-  // (3 x rows x nkp), and the exchanges (3 x rows x padded stride), which either reuse
-  // the stage (FF_B_OVERLAY) or follow the two stages
+  size_t smb = 0;
   const int sh = f64 ? 3 : 4;
-  for (;;) {  // fewer rows per CTA until the stages fit the 227 KB of a CTA
-    size_t stage = 0, exch = 0;
-    for (const auto& q : h->host) {
-      const int H = (int)(q.nx / 2);
-      const size_t rows = (size_t)g.thb * 8 / H;
-      exch = std::max(exch, 3 * rows * (size_t)(H + (H >> sh) + 1));
-      stage = std::max(stage, 3 * rows * (size_t)wq_pitch(q.nkd, es));
-    }
-    const size_t m = 16 / es;
-    if (FF_B_OVERLAY) {
-      stage = std::max(stage, exch);
-      stage = (stage + m - 1) / m * m;
-      g.smb = 128 + 2 * stage * es;
-    } else {
-      stage = (stage + m - 1) / m * m;
-      g.smb = 128 + (2 * stage + exch) * es;
-    }
-    g.stage_b = (int)stage;
-    if (g.smb <= 227 * 1024 || g.thb <= std::max(32, hx / 8)) break;
-    g.thb /= 2;
-    g.tlr = g.thb * 8 / hx;
+  for (const auto& q : h->host) {
+    const int H = (int)(q.nx / 2);
+    const size_t rows = (size_t)g.thb * 8 / H;
+    smb = std::max(smb, 3 * rows * (size_t)(H + (H >> sh) + 1) * es);
   }
+  g.smb = smb;
   return g;
 }
 
@@ -338,8 +318,7 @@ int launch_a(const ff_vort* h, const void* probs, const void* work, int nwork, i
 
 template <typename T>
 int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, cudaStream_t s) {
-  return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg, h->g.stage_b, h->d_status}, probs,
-                          work, nwork, s);
+  return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg}, probs, work, nwork, s);
 }
 
 template <typename T, int EPI>
@@ -435,7 +414,7 @@ void destroy(ff_vort* h) {
   if (h->graph) cudaGraphDestroy(h->graph);
   for (void* p : h->tables) cudaFree(p);
   for (void* p : {h->d_probs, h->d_calc_prob, h->d_work_a, h->d_work_b, h->d_work_c, h->d_calc_work, h->d_inputs,
-                  h->d_calc_input, h->d_W, h->d_Q, (void*)h->d_status})
+                  h->d_calc_input, h->d_W, h->d_Q})
     if (p) cudaFree(p);
   delete h;
 }
@@ -491,8 +470,6 @@ int ff_vort_create(int prec, int stepper, int filtered, double dt, int64_t nprob
   int st = FF_OK;
   cudaError_t e = cudaMalloc(&h->d_W, 3 * wsize * es);
   if (e == cudaSuccess) e = cudaMalloc(&h->d_Q, 2 * wsize * es);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_status, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(int));
   if (e != cudaSuccess) st = cuda_status(e, "ff_vort_create: workspace");
   if (st == FF_OK) {
     const char* nog = getenv("FF_NO_GRAPH");
@@ -509,16 +486,6 @@ int ff_vort_create(int prec, int stepper, int filtered, double dt, int64_t nprob
 
 int ff_vort_destroy(ff_vort* h) {
   destroy(h);
-  return FF_OK;
-}
-
-int ff_vort_status(ff_vort* h, int32_t* flags) {
-  FF_CHECK_ARG(h && flags, "ff_vort_status: null argument");
-  int v = 0;
-  FF_CUDA(cudaDeviceSynchronize());
-  FF_CUDA(cudaMemcpy(&v, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-  FF_CUDA(cudaMemset(h->d_status, 0, sizeof(int)));
-  *flags = v;
   return FF_OK;
 }
 

@@ -116,12 +116,6 @@ class FusedStepper:
     def calcN(self, N, sol, prob=0, stream=None):
         _lib.call("ff_vort_calcN", self._h, int(prob), ptr(sol, "sol"), ptr(N, "N"), stream_handle(stream))
 
-    def status(self):
-        """Device status flags since the last call (0: every bounded wait completed)."""
-        flags = C.c_int32()
-        _lib.call("ff_vort_status", self._h, C.byref(flags))
-        return flags.value
-
     def profile(self, reps=10, stream=None):
         """Average device ms of passes A, B, C (CUDA events inside the library)."""
         ms = (C.c_double * 3)()

@@ -242,12 +242,6 @@ int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stre
  * ETDRK4 and RK4 writes only the stepper's intermediate buffers. */
 int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]);
 
-/* Device status of the handle's kernels since the last call (synchronises the device):
- * 0, or FF_DEV_WAIT_TIMEOUT (1) if a kernel's bounded wait for a bulk copy into shared
- * memory ran out and the kernel returned early (its outputs are then invalid).  Clears the
- * status.  No counterpart in FourierFlows.jl. */
-#define FF_DEV_WAIT_TIMEOUT 1
-int ff_vort_status(ff_vort* h, int32_t* flags);
 
 /* ---- discrete adjoint of the 2D vorticity term and of an ETDRK4 step -------------------- */
 /* No counterpart in FourierFlows.jl (whose gradients would come from an AD system through
