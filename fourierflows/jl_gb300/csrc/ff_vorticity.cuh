@@ -258,6 +258,104 @@ __device__ __forceinline__ void epilogue(const VortProb<T>& P, const EpiScalars<
   }
 }
 
+// The epilogue split into its loads and its arithmetic, so that a thread can issue the
+// loads of several elements before the first store: the output arrays may alias the
+// inputs as far as the compiler knows, so element by element every load would wait for
+// the previous element's stores (one memory round trip per element).
+template <typename T> struct EpiIn {
+  cx<T> x, n1, n2, n3;     // sol or s1, and the stored nonlinear terms
+  T a, b, c, d, fl;        // coefficients (by epilogue) and the filter
+};
+
+template <typename T, int EPI>
+__device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e) {
+  EpiIn<T> in;
+  if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
+    in.x = P.sol[e];
+    in.a = P.eh[e];
+    in.b = P.zc[e];
+  } else if (EPI == EPI_ETD3) {
+    in.x = P.s1[e];
+    in.n1 = P.n1[e];
+    in.a = P.eh[e];
+    in.b = P.zc[e];
+  } else if (EPI == EPI_ETD4) {
+    in.x = P.sol[e];
+    in.n1 = P.n1[e];
+    in.n2 = P.n2[e];
+    in.n3 = P.n3[e];
+    in.a = P.eL[e];
+    in.b = P.al[e];
+    in.c = P.be[e];
+    in.d = P.ga[e];
+  } else if (EPI == EPI_RK1 || EPI == EPI_LS) {
+    in.x = P.sol[e];
+    in.a = P.L[e];
+    if (EPI == EPI_LS && !S.first) in.n1 = P.s1[e];
+  } else if (EPI == EPI_RK2 || EPI == EPI_RK3) {
+    in.x = P.s1[e];
+    in.n1 = P.sol[e];
+    in.a = P.L[e];
+  } else if (EPI == EPI_RK4) {
+    in.x = P.s1[e];
+    in.n1 = P.n1[e];
+    in.n2 = P.n2[e];
+    in.n3 = P.n3[e];
+    in.n3 = P.n3[e];
+    in.a = P.L[e];
+  }
+  if ((EPI == EPI_ETD4 || EPI == EPI_RK4 || EPI == EPI_LS) && S.use_filter) in.fl = P.filter[e];
+  return in;
+}
+
+// the same arithmetic, in the same order, as epilogue<T, EPI>
+template <typename T, int EPI>
+__device__ __forceinline__ void epi_store(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e, cx<T> N,
+                                          const EpiIn<T>& in) {
+  if (EPI == EPI_N) {
+    P.n1[e] = N;
+  } else if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
+    (EPI == EPI_ETD1 ? P.n1 : P.n2)[e] = N;
+    (EPI == EPI_ETD1 ? P.s1 : P.s2)[e] = add(scl(in.x, in.a), scl(N, in.b));
+  } else if (EPI == EPI_ETD3) {
+    P.n3[e] = N;
+    P.s2[e] = add(scl(in.x, in.a), scl(sub(scl(N, T(2)), in.n1), in.b));
+  } else if (EPI == EPI_ETD4) {
+    cx<T> v = add(scl(in.x, in.a), scl(in.n1, in.b));
+    v = add(v, scl(scl(add(in.n2, in.n3), in.c), T(2)));
+    v = add(v, scl(N, in.d));
+    if (S.use_filter) v = scl(v, in.fl);
+    P.sol[e] = v;
+  } else if (EPI == EPI_RK1) {
+    const cx<T> r = add(N, scl(in.x, in.a));
+    P.n1[e] = r;
+    P.s1[e] = add(in.x, scl(r, S.c));
+  } else if (EPI == EPI_RK2 || EPI == EPI_RK3) {
+    const cx<T> r = add(N, scl(in.x, in.a));
+    (EPI == EPI_RK2 ? P.n2 : P.n3)[e] = r;
+    P.s1[e] = add(in.n1, scl(r, S.c));
+  } else if (EPI == EPI_RK4) {
+    const cx<T> r4 = add(N, scl(in.x, in.a));
+    const cx<T> acc = add(add(add(in.n1, scl(in.n2, T(2))), scl(in.n3, T(2))), r4);
+    cx<T> v = add(P.sol[e], scl(acc, S.c));
+    if (S.use_filter) v = scl(v, in.fl);
+    P.sol[e] = v;
+  } else if (EPI == EPI_LS) {
+    const cx<T> r = add(N, scl(in.x, in.a));
+    const cx<T> q = S.first ? scl(r, S.dt) : add(scl(in.n1, S.c), scl(r, S.dt));
+    P.s1[e] = q;
+    cx<T> v = add(in.x, scl(q, S.b));
+    if (S.use_filter) v = scl(v, in.fl);
+    P.sol[e] = v;
+  }
+}
+
+// elements per batch of loads: fewer for the epilogues with many input arrays and in FP64
+template <typename T, int EPI> struct EpiBatch {
+  static constexpr int value =
+      EPI == EPI_LS ? 1 : ((EPI == EPI_ETD4 || EPI == EPI_RK4) ? 4 : 8) / (sizeof(T) == 8 ? 2 : 1);
+};
+
 template <typename T, int EPI>
 __global__ void __launch_bounds__(512) k_vort_c(const VortProb<T>* __restrict__ probs,
                                                 const WorkItem* __restrict__ work, int nwork, int tl,
@@ -461,6 +559,22 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   __syncthreads();
 }
 
+// epilogue of thread t's eight elements (rows t + q NY/8) of column c: the loads of a
+// batch of elements first, then their arithmetic and stores
+template <typename T, int NY, int EPI>
+__device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScalars<T>& S, int c, int t,
+                                             const cx<T> (&N)[8]) {
+  constexpr int PP = NY / 8, QB = EpiBatch<T, EPI>::value;
+#pragma unroll
+  for (int q0 = 0; q0 < 8; q0 += QB) {
+    EpiIn<T> in[QB];
+#pragma unroll
+    for (int b = 0; b < QB; ++b) in[b] = epi_load<T, EPI>(P, S, c + (int64_t)(t + (q0 + b) * PP) * P.nkr);
+#pragma unroll
+    for (int b = 0; b < QB; ++b) epi_store<T, EPI>(P, S, c + (int64_t)(t + (q0 + b) * PP) * P.nkr, N[q0 + b], in[b]);
+  }
+}
+
 template <typename T, int NY, int EPI>
 __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalars<T>& S, int tile, cx<T>* smem) {
   constexpr int PP = NY / 8;
@@ -485,12 +599,15 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
         const int j = t + q * PP;
         cx<T> N = czero<T>();
         if (c < nkd && (j < la || j >= lb)) N = mul_mi(add(scl(v[0][q], P.kr[c]), scl(v[1][q], P.l[j])));
-        epilogue<T, EPI>(P, S, c + j * nkr, N);
+        v[0][q] = N;
       }
+      epilogue_col<T, NY, EPI>(P, S, c, t, v[0]);
     }
   } else if (c < nkr) {
+    cx<T> N[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) epilogue<T, EPI>(P, S, c + (t + q * PP) * nkr, czero<T>());
+    for (int q = 0; q < 8; ++q) N[q] = czero<T>();
+    epilogue_col<T, NY, EPI>(P, S, c, t, N);
   }
 }
 
@@ -503,7 +620,7 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
 #define FF_LB_B_MIN_F32 2
 #endif
 #ifndef FF_LB_C_MIN_F32
-#define FF_LB_C_MIN_F32 2
+#define FF_LB_C_MIN_F32 1
 #endif
 #ifndef FF_LB_A_MIN_F64
 #define FF_LB_A_MIN_F64 (FF_A_FIELDS_F64 == 3 ? 1 : 2)
