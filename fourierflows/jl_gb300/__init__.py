@@ -17,7 +17,8 @@ from .timesteppers import (AB3TimeStepper, AbstractTimeStepper, ETDRK4TimeSteppe
                            FilteredETDRK4TimeStepper, FilteredForwardEulerTimeStepper, FilteredLSRK54TimeStepper,
                            FilteredRK4TimeStepper, ForwardEulerTimeStepper, LSRK54TimeStepper, RK4TimeStepper,
                            TimeStepper, getetdcoeffs, getexpLs, isexplicit, step_until_, stepforward_)
-from .utils import innereltype, jacobian, jacobianh, on_grid, parsevalsum, parsevalsum2, superzeros
+from .utils import (innereltype, jacobian, jacobianh, on_grid, parsevalsum, parsevalsum2, radialspectrum,
+                    superzeros)
 from .diagnostics import AbstractDiagnostic, Diagnostic, extend_, increment_, update_
 from . import diffusion as Diffusion
 from . import vorticity as Vorticity

@@ -65,6 +65,7 @@ SIGNATURES = {
     "ff_real_mul": [i32, i64, i64, vp, vp, vp],
     "ff_parsevalsum2": [i32, vp, i64, i64, i32, f64, C.POINTER(f64), vp],
     "ff_parsevalsum": [i32, vp, i64, i64, i32, f64, C.POINTER(f64), vp],
+    "ff_radialspectrum": [i32, i32, vp, i64, i64, i64, f64, f64, i64, i64, vp, vp],
     "ff_parsevalsum2_weighted": [i32, vp, vp, i64, i64, i32, f64, C.POINTER(f64), vp, vp],
     "ff_vort_velocities": [i32, i64, i64, vp, vp, vp, vp, vp, vp, vp],
     "ff_vort_create": [i32, i32, i32, f64, i64, vp, C.POINTER(vp)],

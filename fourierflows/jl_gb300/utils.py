@@ -6,7 +6,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .devices import CPU, GPU, cxtype, device_array, fltype, on_device, prec_of, ptr, stream_handle, to_numpy, zeros
+from .devices import (CPU, GPU, cxtype, device_array, fltype, np_dtype, on_device, prec_of, ptr, stream_handle,
+                      to_numpy, zeros)
 from .plans import fft, ifft, irfft, rfft
 
 
@@ -90,6 +91,34 @@ def jacobian(a, b, grid):
     if not a.dtype.is_complex:
         return irfft(jacobianh(a, b, grid), grid.nx)
     return ifft(jacobianh(a, b, grid))
+
+
+def radialspectrum(fh, grid, n=None, m=None, refinement=2, stream=None):
+    """(rho, fhr): fh on a TwoDGrid interpolated onto a polar grid and integrated over
+    angle, fhr = [2] rho int fh(rho, theta) dtheta (src/utils.jl:239-283), one native
+    binned reduction (``ff_radialspectrum``).  fh is the conjugate-symmetric (nkr, nl) or
+    full (nk, nl) form, real or complex, on the GPU; rho is returned on the host (the
+    reference's range), fhr on the device with fh's element type."""
+    from .domains import TwoDGrid
+    if not isinstance(grid, TwoDGrid):
+        raise TypeError("radialspectrum is defined for a TwoDGrid (src/utils.jl:239)")
+    if not on_device(fh):
+        raise ValueError("radialspectrum: fh must be a GPU array")
+    n = refinement * max(grid.nk, grid.nl) if n is None else int(n)
+    m = refinement * max(grid.nk, grid.nl) if m is None else int(m)
+    if fh.shape[0] == grid.nkr:
+        if m % 2:
+            raise ValueError("radialspectrum: m must be even for the conjugate-symmetric form")
+        m //= 2
+    elif fh.shape[0] != grid.nk:
+        raise ValueError(f"radialspectrum: fh of size {tuple(fh.shape)} on a {grid.nx} x {grid.ny} grid")
+    if tuple(fh.shape[1:]) != (grid.nl,):
+        raise ValueError(f"radialspectrum: fh of size {tuple(fh.shape)} on a {grid.nx} x {grid.ny} grid")
+    out = zeros(grid.device, np_dtype(fh.dtype), (n,))
+    _lib.call("ff_radialspectrum", prec_of(fh.dtype), 1 if fh.dtype.is_complex else 0, ptr(fh, "fh"), fh.shape[0],
+              grid.nk, grid.nl, float(grid.Lx), float(grid.Ly), n, m, ptr(out, "out"), stream_handle(stream))
+    rhomax = min((grid.nk / 2 - 1) * 2 * np.pi / float(grid.Lx), (grid.nl / 2 - 1) * 2 * np.pi / float(grid.Ly))
+    return np.linspace(0.0, rhomax, n), out
 
 
 def on_grid(func, grid):

@@ -174,6 +174,17 @@ int ff_parsevalsum(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft
 int ff_parsevalsum2_weighted(int prec, const void* uh, const void* wt, int64_t n0, int64_t nrest, int rfft_form,
                              double norm, double* out, double* dev_out, void* stream);
 
+/* radialspectrum(fh, grid; n, m) (src/utils.jl:239-283) for a TwoDGrid nk x nl with
+ * domain Lx x Ly: fh is (n0, nl) with n0 = nk/2 + 1 (conjugate-symmetric form, angles
+ * in [-pi/2, pi/2]) or n0 = nk (full form, angles in [0, 2 pi]), real or complex
+ * (is_complex) in the given precision.  out[i] = [2] rho_i sum_j fh(rho_i, theta_j)
+ * dtheta over `ntheta` angles (the reference's m, halved for the conjugate-symmetric
+ * form), rho_i = i rhomax / (nrho - 1), rhomax = min((nk/2 - 1) 2pi/Lx, (nl/2 - 1)
+ * 2pi/Ly), with fh bilinearly interpolated from its fftshifted layout; out[0] = fh[0].
+ * out has nrho elements of fh's type; sums are FP64. */
+int ff_radialspectrum(int prec, int is_complex, const void* fh, int64_t n0, int64_t nk, int64_t nl, double Lx,
+                      double Ly, int64_t nrho, int64_t ntheta, void* out, void* stream);
+
 /* parsevalsum2 that allocates no device memory.  No counterpart in the reference: it
  * serves callers that cannot call cudaMalloc because another allocator owns the GPU's
  * memory (a pooling allocator that has reserved it, or a fixed-budget embedded code).

@@ -585,6 +585,47 @@ def jacobian(a, b, g):
     return ifft(jacobianh(a, b, g))
 
 
+def _lin_interp_index(x, x0, dx, n):
+    """0-based lower index and weight of linear interpolation on the uniform grid
+    x0 + i dx, i = 0..n-1 (Interpolations.jl's scaled BSpline(Linear()) inside its range)."""
+    u = (x - x0) / dx
+    i = np.clip(np.floor(u).astype(np.int64), 0, n - 2)
+    return i, u - i
+
+
+def radialspectrum(fh, g, n=None, m=None, refinement=2):
+    """src/utils.jl:239-283: fh (rfft form (nkr, nl) or full form (nk, nl)) bilinearly
+    interpolated from its fftshifted layout onto a polar (rho, theta) grid and integrated
+    over theta: fhr = [2] rho sum_theta fh(rho, theta) dtheta, fhr[0] = fh[0, 0].
+    Returns (rho, fhr)."""
+    n = refinement * max(g.nk, g.nl) if n is None else n
+    m = refinement * max(g.nk, g.nl) if m is None else m
+    lshift = np.linspace(-g.nl / 2, g.nl / 2 - 1, g.nl) * 2 * np.pi / g.Ly
+    if fh.shape[0] == g.nkr:
+        m = m // 2
+        theta = np.linspace(-np.pi / 2, np.pi / 2, m)
+        fhs = np.fft.fftshift(fh, axes=1)
+        kshift = np.linspace(0, g.nkr - 1, g.nkr) * 2 * np.pi / g.Lx
+        fac = 2.0
+    else:
+        theta = np.linspace(0, 2 * np.pi, m)
+        fhs = np.fft.fftshift(fh, axes=(0, 1))
+        kshift = np.linspace(-g.nk / 2, g.nk / 2 - 1, g.nk) * 2 * np.pi / g.Lx
+        fac = 1.0
+    rhomax = min((g.nk / 2 - 1) * 2 * np.pi / g.Lx, (g.nl / 2 - 1) * 2 * np.pi / g.Ly)
+    rho = np.linspace(0, rhomax, n)
+    R, TH = np.meshgrid(rho[1:], theta, indexing="ij")
+    i, wi = _lin_interp_index(R * np.cos(TH), kshift[0], kshift[1] - kshift[0], len(kshift))
+    j, wj = _lin_interp_index(R * np.sin(TH), lshift[0], lshift[1] - lshift[0], len(lshift))
+    vals = ((1 - wi) * (1 - wj) * fhs[i, j] + wi * (1 - wj) * fhs[i + 1, j] + (1 - wi) * wj * fhs[i, j + 1]
+            + wi * wj * fhs[i + 1, j + 1])
+    dtheta = theta[1] - theta[0]
+    fhr = np.zeros(n, dtype=np.result_type(fh.dtype, np.float64))
+    fhr[1:] = fac * rho[1:] * vals.sum(axis=1) * dtheta
+    fhr[0] = fh[0, 0]
+    return rho, fhr
+
+
 # ----------------------------------------------------------------------------------------
 # 2D vorticity (the nonlinear term defined for this path; not in FourierFlows.jl)
 # ----------------------------------------------------------------------------------------

@@ -225,3 +225,29 @@ def test_vorticity_tangent_matches_central_differences():
     sm, _ = orc.etdrk4_vorticity_tangent_step(s - h * ds, ds, ts, g)
     fd = (sp - sm) / (2 * h)
     assert np.linalg.norm(fd - tan) / np.linalg.norm(tan) < 1e-8
+
+
+# radialspectrum known answers (test/runtests.jl:297-307 via test/test_utils.jl:59-77):
+# normalised difference to the analytic angular integral below atol 0.1 at refinement 16
+def _radial_cases():
+    d = 128 / 10
+    iso = (lambda k, l: np.exp(-(k ** 2 + l ** 2) / (2 * d ** 2)), lambda r: 2 * np.pi * r * np.exp(-r ** 2 / (2 * d ** 2)))
+
+    def ani_f(k, l):
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return np.exp(-(k ** 2 + l ** 2) / (2 * d ** 2)) * k ** 2 / (k ** 2 + l ** 2)
+
+    ani = (ani_f, lambda r: np.pi * r * np.exp(-r ** 2 / (2 * d ** 2)))
+    return [("isotropic", *iso), ("anisotropic", *ani)]
+
+
+@pytest.mark.parametrize("rfft_form", [False, True])
+@pytest.mark.parametrize("case", [0, 1])
+def test_pin_radialspectrum(rfft_form, case):
+    name, f, fr = _radial_cases()[case]
+    g = orc.Grid(2, (128, 128), (2 * math.pi, 2 * math.pi))
+    K = g.kr if rfft_form else g.k
+    ah = f(K + 0 * g.l, 0 * K + g.l).astype(np.float64)
+    ah[0, 0] = 0.0
+    rho, est = orc.radialspectrum(ah, g, refinement=16)
+    assert np.sum(np.abs(fr(rho) - est)) / len(rho) < 0.1, name
