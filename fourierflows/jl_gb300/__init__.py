@@ -23,6 +23,7 @@ from .diagnostics import AbstractDiagnostic, Diagnostic, extend_, increment_, up
 from . import diffusion as Diffusion
 from . import vorticity as Vorticity
 from . import adjoint as Adjoint
+from .output import Output, flush, openoutput, savediagnostic, saveoutput, saveproblem, uniquepath, withoutjld2
 from .adjoint import rrule_stepforward
 
 __version__ = "0.1.0"
