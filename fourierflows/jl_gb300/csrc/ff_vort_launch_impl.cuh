@@ -42,8 +42,17 @@ int vort_launch_b(const PassLaunch& L, const void* probs, const void* work, int 
 template <typename T, int EPI>
 static void launch_c_epi(const PassLaunch& L, const VortProb<T>* P, const WorkItem* work, int nwork,
                          const EpiScalars<T>& S, cudaStream_t s) {
-  if (L.reg) k_vort_c_r<T, EPI><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, S);
-  else k_vort_c<T, EPI><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, L.tile, S);
+  if (L.reg) {
+    if constexpr (EPI != EPI_N && EPI != EPI_ETD4 && EPI != EPI_RK4) {
+      if (L.fuse) {
+        k_vort_c_r<T, EPI, true><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, S);
+        return;
+      }
+    }
+    k_vort_c_r<T, EPI, false><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, S);
+  } else {
+    k_vort_c<T, EPI><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, L.tile, S);
+  }
 }
 
 template <typename T>
@@ -70,10 +79,17 @@ template <typename T> const void* vort_kernel_a(bool reg) {
 template <typename T> const void* vort_kernel_b(bool reg) {
   return reg ? (const void*)k_vort_b_r<T> : (const void*)k_vort_b<T>;
 }
-template <typename T> const void* vort_kernel_c(bool reg, int epi) {
+template <typename T, int EPI> static const void* fuse_ptr(bool fuse) {
+  if constexpr (EPI != EPI_N && EPI != EPI_ETD4 && EPI != EPI_RK4) {
+    if (fuse) return (const void*)k_vort_c_r<T, EPI, true>;
+  }
+  return (const void*)k_vort_c_r<T, EPI, false>;
+}
+
+template <typename T> const void* vort_kernel_c(bool reg, int epi, bool fuse) {
   switch (epi) {
 #define FF_EPI_PTR(E) \
-  case E: return reg ? (const void*)k_vort_c_r<T, E> : (const void*)k_vort_c<T, E>;
+  case E: return !reg ? (const void*)k_vort_c<T, E> : fuse_ptr<T, E>(fuse);
     FF_EPI_PTR(EPI_N) FF_EPI_PTR(EPI_ETD1) FF_EPI_PTR(EPI_ETD2) FF_EPI_PTR(EPI_ETD3) FF_EPI_PTR(EPI_ETD4)
     FF_EPI_PTR(EPI_RK1) FF_EPI_PTR(EPI_RK2) FF_EPI_PTR(EPI_RK3) FF_EPI_PTR(EPI_RK4) FF_EPI_PTR(EPI_LS)
 #undef FF_EPI_PTR
@@ -88,6 +104,6 @@ template <typename T> const void* vort_kernel_c(bool reg, int epi) {
                                 cudaStream_t);                                                                   \
   template const void* vort_kernel_a<T>(bool);                                                                   \
   template const void* vort_kernel_b<T>(bool);                                                                   \
-  template const void* vort_kernel_c<T>(bool, int);
+  template const void* vort_kernel_c<T>(bool, int, bool);
 
 }  // namespace ff

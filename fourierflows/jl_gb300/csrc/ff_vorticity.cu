@@ -129,7 +129,8 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
   g.tlc = g.thc * 8 / ny;
   g.tlr = g.thb * 8 / hx;
   g.sma = 9 * (size_t)AFields<T>::value * g.tha * es;
-  g.smc = 2 * 9 * (size_t)g.thc * es;
+  // pass C's exchanges: its own two fields, or the fused pass A's fields if more
+  g.smc = (size_t)std::max(2, FuseA<T>::value ? AFields<T>::value : 2) * 9 * (size_t)g.thc * es;
   size_t smb = 0;
   const int sh = f64 ? 3 : 4;
   for (const auto& q : h->host) {
@@ -299,10 +300,12 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   if (int st = ensure_smem(ka, geom.sma)) return st;
   if (int st = ensure_smem(kb, geom.smb)) return st;
   for (int e = 0; e < kNumEpilogues; ++e)
-    if (int st = ensure_smem(vort_kernel_c<T>(geom.reg, e), geom.smc)) return st;
+    for (bool fuse : {false, true})
+      if (int st = ensure_smem(vort_kernel_c<T>(geom.reg, e, fuse), geom.smc)) return st;
   h->g.ga = grid_for<T>(ka, geom.tha, geom.sma, h->nwork_a);
   h->g.gb = grid_for<T>(kb, geom.thb, geom.smb, h->nwork_b);
-  h->g.gc = grid_for<T>(vort_kernel_c<T>(geom.reg, EPI_ETD1), geom.thc, geom.smc, h->nwork_c);
+  h->g.gc = grid_for<T>(vort_kernel_c<T>(geom.reg, EPI_ETD1, geom.reg && FuseA<T>::value), geom.thc, geom.smc,
+                        h->nwork_c);
   if (h->exec) { cudaGraphExecDestroy(h->exec); h->exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
   return FF_OK;
@@ -323,18 +326,24 @@ int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, i
 
 template <typename T, int EPI>
 int launch_c(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, EpiScalars<T> S,
-             cudaStream_t s) {
+             cudaStream_t s, bool fuse = false) {
   const EpiArgs a{(double)S.c, (double)S.b, (double)S.dt, S.first, S.use_filter};
-  return vort_launch_c<T>(PassLaunch{grid, h->g.thc, h->g.smc, h->g.tlc, h->g.reg}, EPI, probs, work, nwork, a,
-                          s);
+  PassLaunch L{grid, h->g.thc, h->g.smc, h->g.tlc, h->g.reg};
+  L.fuse = fuse;
+  return vort_launch_c<T>(L, EPI, probs, work, nwork, a, s);
 }
 
-// one calcN! (passes A, B, C) with epilogue EPI on all problems; `inputs` = pass-A sources
+// One substep's calcN! with epilogue EPI on all problems; `inputs` = pass-A sources.
+// On the register path the substep's pass A ran already, fused into the previous
+// substep's pass C (first = false), and pass C runs the next substep's pass A unless
+// this is the step's last substep (last).
 template <typename T, int EPI>
-int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s) {
-  if (int st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, inputs, s)) return st;
+int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s, bool first = true, bool last = true) {
+  const bool fused = h->g.reg && FuseA<T>::value;
+  if (!fused || first)
+    if (int st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, inputs, s)) return st;
   if (int st = launch_b<T>(h, h->d_probs, h->d_work_b, h->nwork_b, h->g.gb, s)) return st;
-  return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
+  return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s, fused && !last);
 }
 
 template <typename T> int enqueue_step(const ff_vort* h, cudaStream_t s) {
@@ -346,23 +355,23 @@ template <typename T> int enqueue_step(const ff_vort* h, cudaStream_t s) {
   int st = FF_OK;
   if (h->stepper == FF_STEP_ETDRK4) {
     S.use_filter = 0;
-    if ((st = calc<T, EPI_ETD1>(h, in, S, s))) return st;
-    if ((st = calc<T, EPI_ETD2>(h, in + stride, S, s))) return st;
-    if ((st = calc<T, EPI_ETD3>(h, in + 2 * stride, S, s))) return st;
+    if ((st = calc<T, EPI_ETD1>(h, in, S, s, true, false))) return st;
+    if ((st = calc<T, EPI_ETD2>(h, in + stride, S, s, false, false))) return st;
+    if ((st = calc<T, EPI_ETD3>(h, in + 2 * stride, S, s, false, false))) return st;
     S.use_filter = h->filtered ? 1 : 0;
-    return calc<T, EPI_ETD4>(h, in + 3 * stride, S, s);
+    return calc<T, EPI_ETD4>(h, in + 3 * stride, S, s, false, true);
   }
   if (h->stepper == FF_STEP_RK4) {
     const T half = (T)(dt / T(2));
     S.use_filter = 0;
     S.c = half;
-    if ((st = calc<T, EPI_RK1>(h, in, S, s))) return st;
-    if ((st = calc<T, EPI_RK2>(h, in + stride, S, s))) return st;
+    if ((st = calc<T, EPI_RK1>(h, in, S, s, true, false))) return st;
+    if ((st = calc<T, EPI_RK2>(h, in + stride, S, s, false, false))) return st;
     S.c = dt;
-    if ((st = calc<T, EPI_RK3>(h, in + 2 * stride, S, s))) return st;
+    if ((st = calc<T, EPI_RK3>(h, in + 2 * stride, S, s, false, false))) return st;
     S.c = (T)(dt / T(6));
     S.use_filter = h->filtered ? 1 : 0;
-    return calc<T, EPI_RK4>(h, in + 3 * stride, S, s);
+    return calc<T, EPI_RK4>(h, in + 3 * stride, S, s, false, true);
   }
   // LSRK54: Carpenter-Kennedy 2N-storage stages
   for (int i = 0; i < 5; ++i) {
@@ -371,7 +380,7 @@ template <typename T> int enqueue_step(const ff_vort* h, cudaStream_t s) {
     S.dt = dt;
     S.first = i == 0;
     S.use_filter = (i == 4 && h->filtered) ? 1 : 0;
-    if ((st = calc<T, EPI_LS>(h, in, S, s))) return st;
+    if ((st = calc<T, EPI_LS>(h, in, S, s, i == 0, i == 4))) return st;
   }
   return FF_OK;
 }

@@ -33,8 +33,22 @@
 #ifndef FF_A_FIELDS_F64
 #define FF_A_FIELDS_F64 1
 #endif
+// Register path: pass C also runs the next substep's pass A (1) or pass A runs apart (0)
+#ifndef FF_FUSE_A_F32
+#define FF_FUSE_A_F32 1
+#endif
+#ifndef FF_FUSE_A_F64
+#define FF_FUSE_A_F64 0
+#endif
 
 namespace ff {
+
+template <typename T> struct AFields;
+template <> struct AFields<float> { static constexpr int value = FF_A_FIELDS_F32; };
+template <> struct AFields<double> { static constexpr int value = FF_A_FIELDS_F64; };
+template <typename T> struct FuseA;
+template <> struct FuseA<float> { static constexpr bool value = FF_FUSE_A_F32 != 0; };
+template <> struct FuseA<double> { static constexpr bool value = FF_FUSE_A_F64 != 0; };
 
 enum Epilogue {
   EPI_N = 0,      // n1 = N (the bare calcN!)
@@ -308,18 +322,22 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
   return in;
 }
 
-// the same arithmetic, in the same order, as epilogue<T, EPI>
+// the same arithmetic, in the same order, as epilogue<T, EPI>; returns the value stored
+// to the array the next substep transforms (s1, s2 or sol; zero for the last substeps)
 template <typename T, int EPI>
-__device__ __forceinline__ void epi_store(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e, cx<T> N,
-                                          const EpiIn<T>& in) {
+__device__ __forceinline__ cx<T> epi_store(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e, cx<T> N,
+                                           const EpiIn<T>& in) {
+  cx<T> next = czero<T>();
   if (EPI == EPI_N) {
     P.n1[e] = N;
   } else if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
     (EPI == EPI_ETD1 ? P.n1 : P.n2)[e] = N;
-    (EPI == EPI_ETD1 ? P.s1 : P.s2)[e] = add(scl(in.x, in.a), scl(N, in.b));
+    next = add(scl(in.x, in.a), scl(N, in.b));
+    (EPI == EPI_ETD1 ? P.s1 : P.s2)[e] = next;
   } else if (EPI == EPI_ETD3) {
     P.n3[e] = N;
-    P.s2[e] = add(scl(in.x, in.a), scl(sub(scl(N, T(2)), in.n1), in.b));
+    next = add(scl(in.x, in.a), scl(sub(scl(N, T(2)), in.n1), in.b));
+    P.s2[e] = next;
   } else if (EPI == EPI_ETD4) {
     cx<T> v = add(scl(in.x, in.a), scl(in.n1, in.b));
     v = add(v, scl(scl(add(in.n2, in.n3), in.c), T(2)));
@@ -329,11 +347,13 @@ __device__ __forceinline__ void epi_store(const VortProb<T>& P, const EpiScalars
   } else if (EPI == EPI_RK1) {
     const cx<T> r = add(N, scl(in.x, in.a));
     P.n1[e] = r;
-    P.s1[e] = add(in.x, scl(r, S.c));
+    next = add(in.x, scl(r, S.c));
+    P.s1[e] = next;
   } else if (EPI == EPI_RK2 || EPI == EPI_RK3) {
     const cx<T> r = add(N, scl(in.x, in.a));
     (EPI == EPI_RK2 ? P.n2 : P.n3)[e] = r;
-    P.s1[e] = add(in.n1, scl(r, S.c));
+    next = add(in.n1, scl(r, S.c));
+    P.s1[e] = next;
   } else if (EPI == EPI_RK4) {
     const cx<T> r4 = add(N, scl(in.x, in.a));
     const cx<T> acc = add(add(add(in.n1, scl(in.n2, T(2))), scl(in.n3, T(2))), r4);
@@ -347,7 +367,9 @@ __device__ __forceinline__ void epi_store(const VortProb<T>& P, const EpiScalars
     cx<T> v = add(in.x, scl(q, S.b));
     if (S.use_filter) v = scl(v, in.fl);
     P.sol[e] = v;
+    next = v;
   }
+  return next;
 }
 
 // elements per batch of loads: fewer for the epilogues with many input arrays and in FP64
@@ -563,7 +585,7 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
 // batch of elements first, then their arithmetic and stores
 template <typename T, int NY, int EPI>
 __device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScalars<T>& S, int c, int t,
-                                             const cx<T> (&N)[8]) {
+                                             const cx<T> (&N)[8], cx<T> (&next)[8]) {
   constexpr int PP = NY / 8, QB = EpiBatch<T, EPI>::value;
 #pragma unroll
   for (int q0 = 0; q0 < 8; q0 += QB) {
@@ -571,11 +593,73 @@ __device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScal
 #pragma unroll
     for (int b = 0; b < QB; ++b) in[b] = epi_load<T, EPI>(P, S, c + (int64_t)(t + (q0 + b) * PP) * P.nkr);
 #pragma unroll
-    for (int b = 0; b < QB; ++b) epi_store<T, EPI>(P, S, c + (int64_t)(t + (q0 + b) * PP) * P.nkr, N[q0 + b], in[b]);
+    for (int b = 0; b < QB; ++b)
+      next[q0 + b] = epi_store<T, EPI>(P, S, c + (int64_t)(t + (q0 + b) * PP) * P.nkr, N[q0 + b], in[b]);
   }
 }
 
-template <typename T, int NY, int EPI>
+// Pass A of the next substep on values a thread already holds: x[q] is the next
+// substep's input at row t + q NY/8 of column c (the epilogue's output), so the fused
+// column pass skips reading it back.  Must be called by the whole CTA.
+template <typename T, int NY>
+__device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, int tl, int ln, const cx<T> (&x)[8],
+                                            cx<T>* smem) {
+  constexpr int PP = NY / 8;
+  const int nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb;
+  const T kc = c < nkd ? P.kr[c] : T(0);
+  const int bsz = (NY + NY / 8) * tl;
+  const int fs = P.nkp * P.ny;
+  cx<T>* Wc = P.W + c;
+  if (AFields<T>::value == 3) {
+    cx<T> v[3][8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int j = t + q * PP;
+      cx<T> z = czero<T>();
+      T ik = T(0), lj = T(0);
+      if (c < nkd && (j < la || j >= lb)) {
+        z = x[q];
+        ik = P.invK[c + j * nkr];
+        lj = P.l[j];
+      }
+      v[0][q] = mul_i(scl(z, lj * ik));
+      v[1][q] = mul_mi(scl(z, kc * ik));
+      v[2][q] = z;
+    }
+    cx<T>* const buf[3] = {smem, smem + bsz, smem + 2 * bsz};
+    regfft<T, 3, NY, 1>(v, t, P.twy, buf, XCol{tl, ln});
+    if (c < nkd) {
+#pragma unroll
+      for (int f = 0; f < 3; ++f)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Wc[f * fs + (t + q * PP) * P.nkp] = v[f][q];
+    }
+  } else {
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      cx<T> v[1][8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int j = t + q * PP;
+        cx<T> z = czero<T>();
+        if (c < nkd && (j < la || j >= lb)) {
+          const T ik = P.invK[c + j * nkr];
+          z = f == 0 ? mul_i(scl(x[q], P.l[j] * ik)) : f == 1 ? mul_mi(scl(x[q], kc * ik)) : x[q];
+        }
+        v[0][q] = z;
+      }
+      cx<T>* const buf[1] = {smem};
+      regfft<T, 1, NY, 1>(v, t, P.twy, buf, XCol{tl, ln});
+      if (c < nkd) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Wc[f * fs + (t + q * PP) * P.nkp] = v[0][q];
+      }
+    }
+  }
+}
+
+// FUSE: also run the next substep's pass A on the new state of this column tile
+template <typename T, int NY, int EPI, bool FUSE>
 __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalars<T>& S, int tile, cx<T>* smem) {
   constexpr int PP = NY / 8;
   const int tl = blockDim.x / PP;
@@ -593,21 +677,21 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
         v[f][q] = c < nkd ? qsrc[f * fstride + (t + q * PP) * P.nkp] : czero<T>();
     cx<T>* const buf2[2] = {smem, smem + (NY + NY / 8) * tl};
     regfft<T, 2, NY, -1>(v, t, P.twy, buf2, XCol{tl, ln});
-    if (c < nkr) {
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int j = t + q * PP;
-        cx<T> N = czero<T>();
-        if (c < nkd && (j < la || j >= lb)) N = mul_mi(add(scl(v[0][q], P.kr[c]), scl(v[1][q], P.l[j])));
-        v[0][q] = N;
-      }
-      epilogue_col<T, NY, EPI>(P, S, c, t, v[0]);
+    for (int q = 0; q < 8; ++q) {
+      const int j = t + q * PP;
+      cx<T> N = czero<T>();
+      if (c < nkd && (j < la || j >= lb)) N = mul_mi(add(scl(v[0][q], P.kr[c]), scl(v[1][q], P.l[j])));
+      v[0][q] = N;
+      v[1][q] = czero<T>();
     }
+    if (c < nkr) epilogue_col<T, NY, EPI>(P, S, c, t, v[0], v[1]);
+    if (FUSE) a_from_regs<T, NY>(P, c, t, tl, ln, v[1], smem);
   } else if (c < nkr) {
-    cx<T> N[8];
+    cx<T> N[8], next[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) N[q] = czero<T>();
-    epilogue_col<T, NY, EPI>(P, S, c, t, N);
+    epilogue_col<T, NY, EPI>(P, S, c, t, N, next);
   }
 }
 
@@ -639,9 +723,6 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
 #ifndef FF_LB_C4_MIN_F64
 #define FF_LB_C4_MIN_F64 FF_LB_C_MIN_F64
 #endif
-template <typename T> struct AFields;
-template <> struct AFields<float> { static constexpr int value = FF_A_FIELDS_F32; };
-template <> struct AFields<double> { static constexpr int value = FF_A_FIELDS_F64; };
 template <typename T> struct RegBudget;  // minimum resident CTAs per SM by precision
 template <> struct RegBudget<float> {
   static constexpr int A = FF_LB_A_MIN_F32, B = FF_LB_B_MIN_F32, C = FF_LB_C_MIN_F32, C4 = FF_LB_C4_MIN_F32;
@@ -715,7 +796,7 @@ __global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restr
   }
 }
 
-template <typename T, int EPI>
+template <typename T, int EPI, bool FUSE>
 __global__ void __launch_bounds__(FF_LB_C) k_vort_c_r(const VortProb<T>* __restrict__ probs,
                                                   const WorkItem* __restrict__ work, int nwork, EpiScalars<T> S) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -725,7 +806,7 @@ __global__ void __launch_bounds__(FF_LB_C) k_vort_c_r(const VortProb<T>* __restr
     const VortProb<T>& P = probs[it.prob];
     switch (P.ny) {
 #define FF_C_CASE(N) \
-  case N: vort_c_reg<T, N, EPI>(P, S, it.tile, smem); break;
+  case N: vort_c_reg<T, N, EPI, FUSE>(P, S, it.tile, smem); break;
       FF_REG_CASES(FF_C_CASE)
 #undef FF_C_CASE
       default: break;
