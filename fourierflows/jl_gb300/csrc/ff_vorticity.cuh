@@ -315,7 +315,6 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
     in.n1 = P.n1[e];
     in.n2 = P.n2[e];
     in.n3 = P.n3[e];
-    in.n3 = P.n3[e];
     in.a = P.L[e];
   }
   if ((EPI == EPI_ETD4 || EPI == EPI_RK4 || EPI == EPI_LS) && S.use_filter) in.fl = P.filter[e];
