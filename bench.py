@@ -141,6 +141,14 @@ def step_bytes_fp(n, es):
     return {"A": a, "B": b, "C1": c1, "C3": c3, "C4": c4, "step": 4 * a + 4 * b + 2 * c1 + c3 + c4}
 
 
+# DRAM bytes (read + write) of one launch of each pass of this workload (1024^2 FP64, one
+# problem), from one ncu capture with cold L2 (profiles/k_vort_passes_fp64_1024.md): the
+# passes read their inputs from DRAM once; their outputs are still in L2 when they end.
+NCU_TRAFFIC = {"A": 5.88e6, "B": 17.37e6, "C": 28.18e6}
+NCU_TRAFFIC_NOTE = ("ncu dram__bytes of one launch, cold L2, same workload; outputs written back after the "
+                    "kernel ends are not in it")
+
+
 def survey_step_bytes(n, s):
     """20 (C + R) + 21 C with C = (n/2+1) n 2 s, R = n^2 s (one read + one write per FFT)."""
     C = (n // 2 + 1) * n * 2 * s
@@ -274,7 +282,8 @@ def our_arm(a):
     t_ms, byts, flops = passes[dom]
     achieved = byts / (t_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": None, "kernel": f"k_vort_{dom.lower()} (pass {dom})", "peak_source": peak_src,
+                "traffic": NCU_TRAFFIC.get(dom), "traffic_note": NCU_TRAFFIC_NOTE,
+                "kernel": f"k_vort_{dom.lower()} (pass {dom})", "peak_source": peak_src,
                 "pass_ms": {"A": tA, "B": tB, "C": tC},
                 "fp64": {"achieved_tflops": flops / (t_ms * 1e-3) / 1e12, "peak_tflops": fp64,
                          "frac": (flops / (t_ms * 1e-3) / 1e12) / fp64 if fp64 else None,
