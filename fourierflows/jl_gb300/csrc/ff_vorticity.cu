@@ -124,7 +124,7 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
   };
   g.tha = threads(g.tla, ny, 512);
   g.thc = threads(g.tlc, ny, 512);
-  g.thb = threads(g.tlr, hx, 256);
+  g.thb = threads(g.tlr, hx, FF_LB_B_THREADS);
   g.tla = g.tha * 8 / ny;
   g.tlc = g.thc * 8 / ny;
   g.tlr = g.thb * 8 / hx;

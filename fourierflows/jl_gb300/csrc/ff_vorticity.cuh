@@ -730,7 +730,11 @@ template <> struct RegBudget<double> {
   static constexpr int A = FF_LB_A_MIN_F64, B = FF_LB_B_MIN_F64, C = FF_LB_C_MIN_F64, C4 = FF_LB_C4_MIN_F64;
 };
 #define FF_LB_A 512, RegBudget<T>::A
-#define FF_LB_B 256, RegBudget<T>::B
+// pass B's largest CTA (threads; a power of two is used up to this bound)
+#ifndef FF_LB_B_THREADS
+#define FF_LB_B_THREADS 256
+#endif
+#define FF_LB_B FF_LB_B_THREADS, RegBudget<T>::B
 #define FF_LB_C 512, ((EPI == EPI_ETD4 || EPI == EPI_RK4) ? RegBudget<T>::C4 : RegBudget<T>::C)
 
 #define FF_REG_CASES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
