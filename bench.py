@@ -59,6 +59,23 @@ def args_():
 # ----------------------------------------------------------------------------------------
 # helpers
 # ----------------------------------------------------------------------------------------
+def replica_time(total_ms, world, device):
+    """The job's timed-region duration: the MAX over ranks of each replica's own (every rank
+    advances an independent problem; no collective on the data path)."""
+    if world == 1:
+        return total_ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms_per_step, world):
+    """Whole-job steps/s: every rank's problem-steps over the slowest rank's time."""
+    return world * 1e3 / ms_per_step
+
+
 def dist_init(gpus):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -262,13 +279,10 @@ def our_arm(a):
     torch.cuda.synchronize()
     total_ms = timed_steps(torch, fs, a.steps, flush)
     torch.cuda.synchronize()
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replica_time(total_ms, world, "cuda")
     clk = clocks.stop()
     ms_per_step = total_ms / a.steps
-    value = world * 1e3 / ms_per_step
+    value = replica_value(ms_per_step, world)
     launches = a.steps * 12
 
     # per-pass device times (events inside the library) and the roofline of the dominant pass
