@@ -74,6 +74,17 @@ def test_fused_paths_vs_oracle(ff, cuda, kernel_path, stepper, n, ny):
     assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
 
 
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredETDRK4", "RK4", "FilteredRK4", "LSRK54", "FilteredLSRK54"])
+@pytest.mark.parametrize("n,ny", [(64, 64), (128, 256)])
+def test_fp32_fused_steppers_vs_oracle(ff, cuda, stepper, n, ny):
+    """FP32 register path, where pass C also runs the next substep's pass A: every stepper
+    against the FP64 oracle after 20 steps."""
+    prob, oprob = make_pair(ff, n, stepper, T=np.float32, ny=ny)
+    ff.stepforward_(prob, 20)
+    orc.stepforward(oprob, 20)
+    assert rel(ff.to_numpy(prob.sol).astype(np.complex128), oprob.sol) < 1e-5
+
+
 def test_calcN_register_path(ff, cuda):
     for n, ny in [(64, 64), (256, 128), (32, 512)]:
         prob, oprob = make_pair(ff, n, "ETDRK4", ny=ny)
