@@ -634,7 +634,7 @@ __device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, 
         for (int q = 0; q < 8; ++q) Wc[f * fs + (t + q * PP) * P.nkp] = v[f][q];
     }
   } else {
-#pragma unroll
+#pragma unroll 1
     for (int f = 0; f < 3; ++f) {
       cx<T> v[1][8];
 #pragma unroll
