@@ -1,6 +1,6 @@
 """CPU oracle for the FourierFlows.jl pseudospectral time-stepping path (TEST INFRASTRUCTURE).
 
-This module is the checker, never the product: only ``tests/``,
+This module checks the product and is never part of it: only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import it.
 The GPU library in ``fourierflows/jl_gb300`` never calls it.
 
