@@ -13,6 +13,7 @@ line-for-line against the Julia sources (paths relative to the FourierFlows.jl t
 * Equation / Clock / Problem                               -- src/problem.jl:11-111
 * Diffusion module                                         -- src/diffusion.jl:44-176
 * parsevalsum2 / parsevalsum / jacobianh / jacobian        -- src/utils.jl:113-218
+* radialspectrum                                           -- src/utils.jl:239-283
 * Diagnostic / increment! / update! / extend!              -- src/diagnostics.jl:8-116
 
 The reference's FFT is FFTW.jl (compat "1", Project.toml:25; no Manifest, so the exact

@@ -1,7 +1,7 @@
 """Pin the CPU oracle to the reference's own known-answer tests (no GPU).
 
 Each test restates a reference test (path:line in the FourierFlows.jl tree) against
-oracle/ff_oracle.py; these are what make the oracle a trustworthy checker for the GPU
+oracle/ff_oracle.py; these are what make the oracle a trustworthy yardstick for the GPU
 parity tests.
 """
 import math
