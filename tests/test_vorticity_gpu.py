@@ -227,3 +227,22 @@ def test_autotune_keeps_results(ff, cuda):
         prob.sol.copy_(start)
         fs.advance(5)
         assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12, cfg
+
+
+def test_long_horizon_energy_enstrophy_series_fp64(ff, cuda):
+    """Over a long horizon (2000 ETDRK4 steps, t = 4, the plain configuration's ν, μ, dt at
+    256²) the FP64 GPU path's energy and enstrophy series match the oracle's, every 100
+    steps, to 1e-10 relative, and the states to 1e-9 (trajectories of this flow stay
+    close in FP64 over this horizon)."""
+    prob, oprob = make_pair(ff, 256, "ETDRK4", nu=1e-4, mu=1e-2, dt=2e-3, seed=2026)
+    worst_E = worst_Z = 0.0
+    for _ in range(20):
+        ff.stepforward_(prob, 100)
+        orc.stepforward(oprob, 100)
+        E, Eo = ff.Vorticity.energy(prob), orc.vorticity_energy(oprob.sol, oprob.grid)
+        Z, Zo = ff.Vorticity.enstrophy(prob), orc.vorticity_enstrophy(oprob.sol, oprob.grid)
+        worst_E = max(worst_E, abs(E - Eo) / Eo)
+        worst_Z = max(worst_Z, abs(Z - Zo) / Zo)
+    assert prob.clock.step == 2000
+    assert worst_E < 1e-10 and worst_Z < 1e-10, (worst_E, worst_Z)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-9
