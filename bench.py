@@ -299,6 +299,9 @@ def our_arm(a):
                 "traffic": NCU_TRAFFIC.get(dom), "traffic_note": NCU_TRAFFIC_NOTE,
                 "kernel": f"k_vort_{dom.lower()} (pass {dom})", "peak_source": peak_src,
                 "pass_ms": {"A": tA, "B": tB, "C": tC},
+                # the whole step against the survey model's bytes (20 (C+R) + 21 C per step)
+                "step_model_gbs": survey_step_bytes(N, 8) * value / world / 1e9,
+                "step_model_frac": survey_step_bytes(N, 8) * value / world / 1e9 / hbm,
                 "fp64": {"achieved_tflops": flops / (t_ms * 1e-3) / 1e12, "peak_tflops": fp64,
                          "frac": (flops / (t_ms * 1e-3) / 1e12) / fp64 if fp64 else None,
                          "peak_source": "measured by ff_fp64_peak in this run"}}
