@@ -5,6 +5,8 @@
 #include <algorithm>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ff_plan.cuh"
 #include "ff_vort_launch.cuh"
 #include "ff_vorticity.cuh"
@@ -337,8 +339,21 @@ int launch_c(const ff_vort* h, const void* probs, const void* work, int nwork, i
 // On the register path the substep's pass A ran already, fused into the previous
 // substep's pass C (first = false), and pass C runs the next substep's pass A unless
 // this is the step's last substep (last).
+// an NVTX range over one substep's launches (host side: visible when the step is enqueued
+// launch by launch, FF_NO_GRAPH=1; a graph replay is one range, see ff_vort_step)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
+constexpr const char* kSubstepName[kNumEpilogues] = {"calcN",        "ETDRK4 substep 1", "ETDRK4 substep 2",
+                                                     "ETDRK4 substep 3", "ETDRK4 substep 4", "RK4 substep 1",
+                                                     "RK4 substep 2",  "RK4 substep 3",    "RK4 substep 4",
+                                                     "LSRK54 stage"};
+
 template <typename T, int EPI>
 int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s, bool first = true, bool last = true) {
+  const NvtxRange range(kSubstepName[EPI]);
   const bool fused = h->g.reg && FuseA<T>::value;
   if (!fused || first)
     if (int st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, inputs, s)) return st;
@@ -502,6 +517,7 @@ int ff_vort_step(ff_vort* h, int64_t nsteps, void* stream) {
   FF_CHECK_ARG(h, "ff_vort_step: null handle");
   FF_CHECK_ARG(nsteps >= 0, "ff_vort_step: negative step count");
   auto s = (cudaStream_t)stream;
+  const NvtxRange range("ff_vort_step");
   if (!h->use_graph) {
     for (int64_t i = 0; i < nsteps; ++i)
       if (int st = enqueue(h, s)) return st;
