@@ -430,6 +430,8 @@ class Ensemble:
     def __init__(self, members, mu=1e-2, dt=2e-3, stepper="ETDRK4", T=np.float32, Lx=2 * math.pi, E0=0.5,
                  k0=6.0, dev=None):
         from .timesteppers import _LSRK_A, _LSRK_B
+        if len(members) == 0:
+            raise ValueError("Ensemble: no members")
         dev = dev if dev is not None else GPU()
         self.T, self.dt, self.stepper = np.dtype(T).type, dt, stepper
         self.grids = {}

@@ -169,3 +169,8 @@ def test_stepper_dispatch_names(ff):
     g = ff.OneDGrid(ff.CPU(), nx=8, Lx=2 * math.pi)
     with pytest.raises(ValueError):
         ff.TimeStepper("Nope", ff.Equation(np.zeros(5), None, g), 0.1, ff.CPU())
+
+
+def test_empty_ensemble_rejected(ff):
+    with pytest.raises(ValueError):
+        ff.Vorticity.Ensemble([])

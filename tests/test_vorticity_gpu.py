@@ -246,3 +246,14 @@ def test_long_horizon_energy_enstrophy_series_fp64(ff, cuda):
     assert prob.clock.step == 2000
     assert worst_E < 1e-10 and worst_Z < 1e-10, (worst_E, worst_Z)
     assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-9
+
+
+@pytest.mark.parametrize("n,ny", [(4096, 32), (32, 4096)])
+def test_register_path_maximum_lengths(ff, cuda, n, ny):
+    """The longest lines the register-resident kernels take: rows of nx/2 = 2048 and
+    columns of ny = 4096, FP64, three ETDRK4 steps against the oracle."""
+    prob, oprob = make_pair(ff, n, "ETDRK4", ny=ny, dt=1e-4)
+    ff.stepforward_(prob, 3)
+    assert prob.timestepper._native(prob.eqn).fs.config()["radix_order"] == -1
+    orc.stepforward(oprob, 3)
+    assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
