@@ -78,6 +78,7 @@ struct ff_vort {
   void* d_inputs = nullptr;     // const cx<T>*[5][nprob]: pass-A inputs per substep
   void* d_calc_input = nullptr;
   int nwork_a = 0, nwork_b = 0, nwork_c = 0;
+  int nwork_c_kept = 0;         // pass C: the kept-column tiles, a prefix of the work list
   std::vector<void*> tables;    // twiddle tables
   void* d_W = nullptr;
   void* d_Q = nullptr;
@@ -265,7 +266,20 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   };
   std::stable_sort(wa.begin(), wa.end(), by_size);
   std::stable_sort(wb.begin(), wb.end(), by_size);
-  std::stable_sort(wc.begin(), wc.end(), by_size);
+  // pass C: tiles of kept columns first (largest problems first), then aliased columns
+  auto kept_then_size = [&](const WorkItem& a, const WorkItem& b) {
+    const int wa_c = geom.reg ? geom.thc * 8 / probs[a.prob].ny : geom.tlc;
+    const int wb_c = geom.reg ? geom.thc * 8 / probs[b.prob].ny : geom.tlc;
+    const bool ka = a.tile * wa_c < probs[a.prob].nkd, kb = b.tile * wb_c < probs[b.prob].nkd;
+    if (ka != kb) return ka;
+    return by_size(a, b);
+  };
+  std::stable_sort(wc.begin(), wc.end(), kept_then_size);
+  h->nwork_c_kept = 0;
+  for (const WorkItem& it : wc) {
+    const int w_c = geom.reg ? geom.thc * 8 / probs[it.prob].ny : geom.tlc;
+    if (it.tile * w_c < probs[it.prob].nkd) ++h->nwork_c_kept;
+  }
   for (void** p : {&h->d_probs, &h->d_work_a, &h->d_work_b, &h->d_work_c, &h->d_inputs})
     if (*p) { cudaFree(*p); *p = nullptr; }
   h->host_desc.resize(sizeof(VortProb<T>) * h->nprob);
@@ -358,7 +372,10 @@ int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s, 
   if (!fused || first)
     if (int st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, inputs, s)) return st;
   if (int st = launch_b<T>(h, h->d_probs, h->d_work_b, h->nwork_b, h->g.gb, s)) return st;
-  return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s, fused && !last);
+  // ETDRK4 substeps 1-3 leave the aliased columns alone on the register path (see k_vort_c_r)
+  const bool kept_only = h->g.reg && (EPI == EPI_ETD1 || EPI == EPI_ETD2 || EPI == EPI_ETD3);
+  return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, kept_only ? h->nwork_c_kept : h->nwork_c, h->g.gc, S, s,
+                          fused && !last);
 }
 
 template <typename T> int enqueue_step(const ff_vort* h, cudaStream_t s) {

@@ -687,10 +687,23 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
     if (c < nkr) epilogue_col<T, NY, EPI>(P, S, c, t, v[0], v[1]);
     if (FUSE) a_from_regs<T, NY>(P, c, t, tl, ln, v[1], smem);
   } else if (c < nkr) {
-    cx<T> N[8], next[8];
+    // aliased kr columns: N1..N4 are zero here, so an ETDRK4 step is sol = expL sol [f].
+    // (Pass C of substeps 1-3 does not visit these tiles: their work list is the prefix
+    // of kept tiles, and the stepper's buffers there are never read.)
+    if (EPI == EPI_ETD4) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) N[q] = czero<T>();
-    epilogue_col<T, NY, EPI>(P, S, c, t, N, next);
+      for (int q = 0; q < 8; ++q) {
+        const int64_t e = c + (int64_t)(t + q * PP) * nkr;
+        cx<T> v = scl(P.sol[e], P.eL[e]);
+        if (S.use_filter) v = scl(v, P.filter[e]);
+        P.sol[e] = v;
+      }
+    } else {
+      cx<T> N[8], next[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) N[q] = czero<T>();
+      epilogue_col<T, NY, EPI>(P, S, c, t, N, next);
+    }
   }
 }
 
