@@ -281,9 +281,22 @@ template <typename T> struct EpiIn {
   T a, b, c, d, fl;        // coefficients (by epilogue) and the filter
 };
 
+// live: false on the aliased l rows of kept columns under ETDRK4, where N is zero and the
+// intermediates are never read: only what the last substep's expL sol [f] needs is loaded
 template <typename T, int EPI>
-__device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e) {
+__device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e,
+                                             bool live = true) {
   EpiIn<T> in;
+  in.x = in.n1 = in.n2 = in.n3 = czero<T>();
+  in.a = in.b = in.c = in.d = in.fl = T(0);
+  if (!live && EPI >= EPI_ETD1 && EPI <= EPI_ETD4) {
+    if (EPI == EPI_ETD4) {
+      in.x = P.sol[e];
+      in.a = P.eL[e];
+      if (S.use_filter) in.fl = P.filter[e];
+    }
+    return in;
+  }
   if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
     in.x = P.sol[e];
     in.a = P.eh[e];
@@ -325,8 +338,9 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
 // to the array the next substep transforms (s1, s2 or sol; zero for the last substeps)
 template <typename T, int EPI>
 __device__ __forceinline__ cx<T> epi_store(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e, cx<T> N,
-                                           const EpiIn<T>& in) {
+                                           const EpiIn<T>& in, bool live = true) {
   cx<T> next = czero<T>();
+  if (!live && EPI >= EPI_ETD1 && EPI <= EPI_ETD3) return next;  // nothing there is read
   if (EPI == EPI_N) {
     P.n1[e] = N;
   } else if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
@@ -590,10 +604,15 @@ __device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScal
   for (int q0 = 0; q0 < 8; q0 += QB) {
     EpiIn<T> in[QB];
 #pragma unroll
-    for (int b = 0; b < QB; ++b) in[b] = epi_load<T, EPI>(P, S, c + (int64_t)(t + (q0 + b) * PP) * P.nkr);
+    for (int b = 0; b < QB; ++b) {
+      const int j = t + (q0 + b) * PP;
+      in[b] = epi_load<T, EPI>(P, S, c + (int64_t)j * P.nkr, j < P.la || j >= P.lb);
+    }
 #pragma unroll
-    for (int b = 0; b < QB; ++b)
-      next[q0 + b] = epi_store<T, EPI>(P, S, c + (int64_t)(t + (q0 + b) * PP) * P.nkr, N[q0 + b], in[b]);
+    for (int b = 0; b < QB; ++b) {
+      const int j = t + (q0 + b) * PP;
+      next[q0 + b] = epi_store<T, EPI>(P, S, c + (int64_t)j * P.nkr, N[q0 + b], in[b], j < P.la || j >= P.lb);
+    }
   }
 }
 
