@@ -372,8 +372,9 @@ int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s, 
   if (!fused || first)
     if (int st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, inputs, s)) return st;
   if (int st = launch_b<T>(h, h->d_probs, h->d_work_b, h->nwork_b, h->g.gb, s)) return st;
-  // ETDRK4 substeps 1-3 leave the aliased columns alone on the register path (see k_vort_c_r)
-  const bool kept_only = h->g.reg && (EPI == EPI_ETD1 || EPI == EPI_ETD2 || EPI == EPI_ETD3);
+  // ETDRK4 / RK4 substeps 1-3 leave the aliased columns alone on the register path (see k_vort_c_r)
+  const bool kept_only = h->g.reg && (EPI == EPI_ETD1 || EPI == EPI_ETD2 || EPI == EPI_ETD3 || EPI == EPI_RK1 ||
+                                      EPI == EPI_RK2 || EPI == EPI_RK3);
   return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, kept_only ? h->nwork_c_kept : h->nwork_c, h->g.gc, S, s,
                           fused && !last);
 }
@@ -396,6 +397,7 @@ template <typename T> int enqueue_step(const ff_vort* h, cudaStream_t s) {
   if (h->stepper == FF_STEP_RK4) {
     const T half = (T)(dt / T(2));
     S.use_filter = 0;
+    S.dt = dt;  // the last substep advances the aliased modes through all four stages
     S.c = half;
     if ((st = calc<T, EPI_RK1>(h, in, S, s, true, false))) return st;
     if ((st = calc<T, EPI_RK2>(h, in + stride, S, s, false, false))) return st;

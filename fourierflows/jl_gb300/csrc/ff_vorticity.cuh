@@ -289,10 +289,10 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
   EpiIn<T> in;
   in.x = in.n1 = in.n2 = in.n3 = czero<T>();
   in.a = in.b = in.c = in.d = in.fl = T(0);
-  if (!live && EPI >= EPI_ETD1 && EPI <= EPI_ETD4) {
-    if (EPI == EPI_ETD4) {
+  if (!live && EPI >= EPI_ETD1 && EPI <= EPI_RK4) {
+    if (EPI == EPI_ETD4 || EPI == EPI_RK4) {
       in.x = P.sol[e];
-      in.a = P.eL[e];
+      in.a = EPI == EPI_ETD4 ? P.eL[e] : P.L[e];
       if (S.use_filter) in.fl = P.filter[e];
     }
     return in;
@@ -340,7 +340,25 @@ template <typename T, int EPI>
 __device__ __forceinline__ cx<T> epi_store(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e, cx<T> N,
                                            const EpiIn<T>& in, bool live = true) {
   cx<T> next = czero<T>();
-  if (!live && EPI >= EPI_ETD1 && EPI <= EPI_ETD3) return next;  // nothing there is read
+  if (!live) {
+    if ((EPI >= EPI_ETD1 && EPI <= EPI_ETD3) || (EPI >= EPI_RK1 && EPI <= EPI_RK3)) return next;  // never read
+    if (EPI == EPI_RK4) {
+      // the four RK4 stages of a mode with N = 0, in the order the substeps take them
+      const T half = S.dt / T(2);
+      const cx<T> n1 = scl(in.x, in.a);
+      cx<T> s1 = add(in.x, scl(n1, half));
+      const cx<T> n2 = scl(s1, in.a);
+      s1 = add(in.x, scl(n2, half));
+      const cx<T> n3 = scl(s1, in.a);
+      s1 = add(in.x, scl(n3, S.dt));
+      const cx<T> r4 = scl(s1, in.a);
+      const cx<T> acc = add(add(add(n1, scl(n2, T(2))), scl(n3, T(2))), r4);
+      cx<T> v = add(in.x, scl(acc, S.c));
+      if (S.use_filter) v = scl(v, in.fl);
+      P.sol[e] = v;
+      return next;
+    }
+  }
   if (EPI == EPI_N) {
     P.n1[e] = N;
   } else if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
@@ -596,9 +614,13 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
 
 // epilogue of thread t's eight elements (rows t + q NY/8) of column c: the loads of a
 // batch of elements first, then their arithmetic and stores
+// Under ETDRK4 and RK4 the aliased modes (c >= nkd or an aliased l row) are "dead": N is
+// zero there, the substeps' intermediates are never read there, and the last substep
+// advances them by the linear part alone.
 template <typename T, int NY, int EPI>
 __device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScalars<T>& S, int c, int t,
                                              const cx<T> (&N)[8], cx<T> (&next)[8]) {
+  const bool col_live = c < P.nkd;
   constexpr int PP = NY / 8, QB = EpiBatch<T, EPI>::value;
 #pragma unroll
   for (int q0 = 0; q0 < 8; q0 += QB) {
@@ -606,12 +628,13 @@ __device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScal
 #pragma unroll
     for (int b = 0; b < QB; ++b) {
       const int j = t + (q0 + b) * PP;
-      in[b] = epi_load<T, EPI>(P, S, c + (int64_t)j * P.nkr, j < P.la || j >= P.lb);
+      in[b] = epi_load<T, EPI>(P, S, c + (int64_t)j * P.nkr, col_live && (j < P.la || j >= P.lb));
     }
 #pragma unroll
     for (int b = 0; b < QB; ++b) {
       const int j = t + (q0 + b) * PP;
-      next[q0 + b] = epi_store<T, EPI>(P, S, c + (int64_t)j * P.nkr, N[q0 + b], in[b], j < P.la || j >= P.lb);
+      next[q0 + b] = epi_store<T, EPI>(P, S, c + (int64_t)j * P.nkr, N[q0 + b], in[b],
+                                       col_live && (j < P.la || j >= P.lb));
     }
   }
 }
@@ -706,23 +729,12 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
     if (c < nkr) epilogue_col<T, NY, EPI>(P, S, c, t, v[0], v[1]);
     if (FUSE) a_from_regs<T, NY>(P, c, t, tl, ln, v[1], smem);
   } else if (c < nkr) {
-    // aliased kr columns: N1..N4 are zero here, so an ETDRK4 step is sol = expL sol [f].
-    // (Pass C of substeps 1-3 does not visit these tiles: their work list is the prefix
-    // of kept tiles, and the stepper's buffers there are never read.)
-    if (EPI == EPI_ETD4) {
+    // aliased kr columns (substeps 1-3 of ETDRK4 and RK4 do not visit these tiles: their
+    // work list is the prefix of kept tiles)
+    cx<T> N[8], next[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int64_t e = c + (int64_t)(t + q * PP) * nkr;
-        cx<T> v = scl(P.sol[e], P.eL[e]);
-        if (S.use_filter) v = scl(v, P.filter[e]);
-        P.sol[e] = v;
-      }
-    } else {
-      cx<T> N[8], next[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) N[q] = czero<T>();
-      epilogue_col<T, NY, EPI>(P, S, c, t, N, next);
-    }
+    for (int q = 0; q < 8; ++q) N[q] = czero<T>();
+    epilogue_col<T, NY, EPI>(P, S, c, t, N, next);
   }
 }
 

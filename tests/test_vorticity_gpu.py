@@ -259,12 +259,13 @@ def test_register_path_maximum_lengths(ff, cuda, n, ny):
     assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12
 
 
-@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredETDRK4"])
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredETDRK4", "RK4", "FilteredRK4", "LSRK54"])
 @pytest.mark.parametrize("T", [np.float64, np.float32])
 def test_state_with_aliased_modes(ff, cuda, stepper, T):
     """A state with energy in the aliased modes (which the nonlinear term never sees and
-    which evolve by expL alone): the fused path skips the aliased columns and rows in the
-    first three substeps and must still match the oracle everywhere."""
+    which evolve by the linear part alone): the fused ETDRK4 and RK4 paths skip the
+    aliased columns and rows in the first three substeps and must still match the oracle
+    everywhere."""
     n, ny = 128, 96
     prob, oprob = make_pair(ff, n, stepper, T=T, ny=ny)
     rng = np.random.default_rng(77)
@@ -278,7 +279,7 @@ def test_state_with_aliased_modes(ff, cuda, stepper, T):
     tol = 1e-12 if T == np.float64 else 1e-5
     assert rel(got, oprob.sol) < tol
     g = prob.grid
-    # the aliased modes alone, against the oracle's (expL^10 s0 there)
+    # the aliased modes alone, against the oracle's
     assert rel(got[g.kralias.start:, :], oprob.sol[g.kralias.start:, :]) < tol
     assert rel(got[:g.kralias.start, g.lalias.start:g.lalias.stop],
                oprob.sol[:g.kralias.start, g.lalias.start:g.lalias.stop]) < tol
