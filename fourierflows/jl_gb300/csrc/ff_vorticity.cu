@@ -622,6 +622,11 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
 }  // extern "C"
 
 template <typename T> int profile_t(ff_vort* h, int reps, cudaStream_t s, double ms[3]) {
+  if (h->stepper != FF_STEP_ETDRK4 && h->stepper != FF_STEP_RK4) {
+    // an LSRK54 stage's epilogue advances the state itself
+    set_error("ff_vort_profile: only ETDRK4 and RK4 handles can be profiled without advancing the state");
+    return FF_ERR_UNSUPPORTED;
+  }
   cudaEvent_t ev[4];
   for (auto& e : ev) FF_CUDA(cudaEventCreate(&e));
   double acc[3] = {0, 0, 0};
@@ -629,15 +634,19 @@ template <typename T> int profile_t(ff_vort* h, int reps, cudaStream_t s, double
   EpiScalars<T> S{};
   S.c = (T)(h->dt / 2);
   for (int r = 0; r < reps && st == FF_OK; ++r) {
-    // pass A on the state, B, then C with the first substep's epilogue (which writes
-    // only the stepper's intermediate buffers for ETDRK4 and RK4)
+    // pass A on the state, B, then C as the first substep runs it (its epilogue writes
+    // only the stepper's intermediate buffers; fused with the next pass A in FP32)
     FF_CUDA(cudaEventRecord(ev[0], s));
     if ((st = launch_a<T>(h, h->d_probs, h->d_work_a, h->nwork_a, h->g.ga, h->d_inputs, s))) break;
     FF_CUDA(cudaEventRecord(ev[1], s));
     if ((st = launch_b<T>(h, h->d_probs, h->d_work_b, h->nwork_b, h->g.gb, s))) break;
     FF_CUDA(cudaEventRecord(ev[2], s));
-    st = h->stepper == FF_STEP_RK4 ? launch_c<T, EPI_RK1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s)
-                                   : launch_c<T, EPI_ETD1>(h, h->d_probs, h->d_work_c, h->nwork_c, h->g.gc, S, s);
+    {
+      const int nw = h->g.reg ? h->nwork_c_kept : h->nwork_c;
+      const bool fuse = h->g.reg && FuseA<T>::value;
+      st = h->stepper == FF_STEP_RK4 ? launch_c<T, EPI_RK1>(h, h->d_probs, h->d_work_c, nw, h->g.gc, S, s, fuse)
+                                     : launch_c<T, EPI_ETD1>(h, h->d_probs, h->d_work_c, nw, h->g.gc, S, s, fuse);
+    }
     if (st) break;
     FF_CUDA(cudaEventRecord(ev[3], s));
     FF_CUDA(cudaEventSynchronize(ev[3]));

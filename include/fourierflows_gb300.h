@@ -249,8 +249,9 @@ int ff_vort_step(ff_vort* h, int64_t nsteps, void* stream);
 int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream);
 
 /* Average device time (ms) of each of the three passes over `reps` launches, timed with
- * CUDA events on `stream`: ms = {A, B, C}; C runs the first substep's epilogue, which for
- * ETDRK4 and RK4 writes only the stepper's intermediate buffers. */
+ * CUDA events on `stream`: ms = {A, B, C}; C runs as in the first substep (its epilogue
+ * writes only the stepper's intermediate buffers).  ETDRK4 and RK4 handles only
+ * (FF_ERR_UNSUPPORTED otherwise: an LSRK54 stage advances the state). */
 int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3]);
 
 

@@ -283,3 +283,20 @@ def test_state_with_aliased_modes(ff, cuda, stepper, T):
     assert rel(got[g.kralias.start:, :], oprob.sol[g.kralias.start:, :]) < tol
     assert rel(got[:g.kralias.start, g.lalias.start:g.lalias.stop],
                oprob.sol[:g.kralias.start, g.lalias.start:g.lalias.stop]) < tol
+
+
+def test_profile_pass_times(ff, cuda):
+    """ff_vort_profile on ETDRK4 and RK4 handles (state untouched); an LSRK54 stage would
+    advance the state, so that handle is refused."""
+    for stepper, T in (("ETDRK4", np.float64), ("ETDRK4", np.float32), ("RK4", np.float32)):
+        prob, _ = make_pair(ff, 64, stepper, T=T)
+        ff.stepforward_(prob, 1)
+        fs = prob.timestepper._native(prob.eqn).fs
+        before = ff.to_numpy(prob.sol)
+        ms = fs.profile(reps=2)
+        assert len(ms) == 3 and all(t > 0 for t in ms)
+        assert np.array_equal(ff.to_numpy(prob.sol), before)
+    prob, _ = make_pair(ff, 64, "LSRK54")
+    ff.stepforward_(prob, 1)
+    with pytest.raises(Exception, match="ETDRK4 and RK4"):
+        prob.timestepper._native(prob.eqn).fs.profile(reps=1)
