@@ -61,6 +61,7 @@ SIGNATURES = {
     "ff_etdrk4_update": [i32, i64, vp, ff_coef, ff_coef, ff_coef, ff_coef, vp, vp, vp, vp, vp, vp],
     "ff_ab3_update": [i32, i64, vp, vp, vp, vp, ff_coef, f64, i32, vp, vp],
     "ff_filter_mul": [i32, i64, vp, vp, vp],
+    "ff_linear_step": [i32, i32, i64, vp, ff_coef, f64, vp, i64, vp],
     "ff_mul_ik": [i32, i64, i64, vp, vp, vp, vp],
     "ff_real_mul": [i32, i64, i64, vp, vp, vp],
     "ff_parsevalsum2": [i32, vp, i64, i64, i32, f64, C.POINTER(f64), vp],

@@ -11,9 +11,12 @@
 // slot that the second launch reads was written by the first launch of the same call, so
 // nothing needs clearing between calls; but all calls share the array, so calls that
 // overlap on the GPU (different streams, or different host threads) race on it.
+#include <cuda.h>  // CUcontext / CUresult types only: driver calls go through the runtime's entry points
+
 #include <mutex>
 
 #include "ff_common.cuh"
+#include "ff_ctx_cache.h"
 
 #define FF_NOALLOC_THREADS 256
 #define FF_NOALLOC_CHUNK 8192                           // modes per CTA
@@ -63,34 +66,62 @@ __global__ void k_noalloc_finish(const double* __restrict__ slots, int nslots, d
   if (threadIdx.x == 0) *out = acc * norm;
 }
 
-// Device address of g_noalloc_partials, looked up once per device with that device current.
-// In host code the symbol names a host-side stand-in, never the device array itself.
-double* scratch_address(int* status) {
-  static std::mutex mu;
-  static double* addr[64] = {nullptr};
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    *status = ff::cuda_status(e, "ff_parsevalsum2_noalloc: cudaGetDevice");
-    return nullptr;
-  }
-  if (dev < 0 || dev >= 64) {
-    ff::set_error("ff_parsevalsum2_noalloc: device index %d out of range", dev);
-    *status = FF_ERR_UNSUPPORTED;
-    return nullptr;
-  }
-  std::lock_guard<std::mutex> lk(mu);
-  if (!addr[dev]) {
+// The current context's unique ID (cuCtxGetId), through driver entry points that the
+// runtime hands out, so the library does not link libcuda itself.  False when no context
+// is current yet or the driver has no context IDs.
+bool current_context_id(unsigned long long* id) {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_cur = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-    if (e != cudaSuccess) {
-      *status = ff::cuda_status(e, "ff_parsevalsum2_noalloc: cudaGetSymbolAddress");
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = (GetCurrent)p;
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)p;
+  });
+  if (!get_cur || !get_id) return false;
+  CUcontext ctx = nullptr;
+  if (get_cur(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+int fetch_scratch(void** p) {
+  const cudaError_t e = cudaGetSymbolAddress(p, g_noalloc_partials);
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
+// Device address of g_noalloc_partials in the current context.  In host code the symbol
+// names a host-side stand-in, never the device array itself.  The address is cached per
+// context ID: after a device reset (or a re-created primary context) the new context has
+// a new ID and the address is looked up again, in that context.
+double* scratch_address(int* status) {
+  static ff::CtxAddressCache<64> cache;
+  unsigned long long id = 0;
+  void* p = nullptr;
+  if (!current_context_id(&id)) {
+    // no current context yet (the runtime makes the primary context current lazily, and
+    // this lookup does so) or no context IDs: look the address up directly
+    if (const int e = fetch_scratch(&p)) {
+      *status = ff::cuda_status((cudaError_t)e, "ff_parsevalsum2_noalloc: cudaGetSymbolAddress");
       return nullptr;
     }
-    addr[dev] = (double*)p;
+    if (current_context_id(&id)) cache.get(id, &p, [p](void** q) { *q = p; return 0; });
+    *status = FF_OK;
+    return (double*)p;
+  }
+  if (const int e = cache.get(id, &p, fetch_scratch)) {
+    *status = ff::cuda_status((cudaError_t)e, "ff_parsevalsum2_noalloc: cudaGetSymbolAddress");
+    return nullptr;
   }
   *status = FF_OK;
-  return addr[dev];
+  return (double*)p;
 }
 
 }  // namespace

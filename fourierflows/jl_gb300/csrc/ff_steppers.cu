@@ -139,6 +139,100 @@ template <typename T> __global__ void k_filter(int64_t n, cx<T>* sol, const T* _
   GRID_STRIDE(i, n) sol[i] = scl(sol[i], f[i]);
 }
 
+// ---- whole steps of a linear equation (N = 0): one pass for nsteps steps -----------------
+// The Diffusion module's constant-kappa calcN! sets N = 0 (src/diffusion.jl:129-133).  An
+// ETDRK4 step then reduces exactly to sol = [filter] exp(L dt) sol: every term in N1..N4
+// of ETDRK4update! adds an exact zero (src/timesteppers.jl:501-504,552).  An RK4 step is
+// its four linear stages, computed in registers in the order the generic kernels take them
+// (k_rk4_substep three times, then k_rk4_update), so both give the generic path's bits.
+template <typename T>
+__global__ void k_linear_etd(int64_t n, cx<T>* sol, Coef<T> eL, const T* __restrict__ filter, int nsteps) {
+  GRID_STRIDE(i, n) {
+    cx<T> v = sol[i];
+    for (int k = 0; k < nsteps; ++k) {
+      v = eL.mul(v, i);
+      if (filter) v = scl(v, filter[i]);
+    }
+    sol[i] = v;
+  }
+}
+
+// FP32 state with a real exp(L dt): two modes per thread per iteration (16-byte state and
+// 8-byte coefficient loads), four iterations in flight per thread
+__global__ void k_linear_etd_f32x2(int64_t npairs, float4* sol, const float2* __restrict__ eL,
+                                   const float2* __restrict__ filter, int nsteps) {
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < npairs; i0 += U * stride) {
+    float4 v[U];
+    float2 e[U], f[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < npairs) {
+        v[u] = sol[i];
+        e[u] = eL[i];
+        f[u] = filter ? filter[i] : make_float2(1.f, 1.f);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < npairs) {
+        float4 x = v[u];
+        for (int k = 0; k < nsteps; ++k) {
+          x.x *= e[u].x;
+          x.y *= e[u].x;
+          x.z *= e[u].y;
+          x.w *= e[u].y;
+          if (filter) {
+            x.x *= f[u].x;
+            x.y *= f[u].x;
+            x.z *= f[u].y;
+            x.w *= f[u].y;
+          }
+        }
+        sol[i] = x;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// L x rounded on its own, as the generic kernels' RHS = N + L x with N = 0 rounds it: a
+// bare product must not be contracted into the add that consumes it
+template <typename T> __device__ __forceinline__ cx<T> lin(const Coef<T>& L, cx<T> v, int64_t i) {
+  if (L.kind == FF_COEF_REAL) {
+    const T c = static_cast<const T*>(L.p)[i];
+    return mk<T>(mul_rn(v.x, c), mul_rn(v.y, c));
+  }
+  if (L.kind == FF_COEF_SCALAR && L.im == T(0)) return mk<T>(mul_rn(v.x, L.re), mul_rn(v.y, L.re));
+  return L.mul(v, i);
+}
+
+template <typename T>
+__global__ void k_linear_rk4(int64_t n, cx<T>* sol, Coef<T> L, T half, T dt, T c6, const T* __restrict__ filter,
+                             int nsteps) {
+  GRID_STRIDE(i, n) {
+    cx<T> s = sol[i];
+    for (int k = 0; k < nsteps; ++k) {
+      const cx<T> r1 = lin(L, s, i);
+      cx<T> x = add(s, scl(r1, half));
+      const cx<T> r2 = lin(L, x, i);
+      x = add(s, scl(r2, half));
+      const cx<T> r3 = lin(L, x, i);
+      x = add(s, scl(r3, dt));
+      const cx<T> r4 = lin(L, x, i);
+      const cx<T> acc = add(add(add(r1, scl(r2, T(2))), scl(r3, T(2))), r4);
+      s = add(s, scl(acc, c6));
+      if (filter) s = scl(s, filter[i]);
+    }
+    sol[i] = s;
+  }
+}
+
 template <typename T>
 __global__ void k_dealias(cx<T>* fh, int64_t d0, int64_t d1, int64_t d2, int64_t total, int64_t lo0, int64_t hi0,
                           int64_t lo1, int64_t hi1, int64_t lo2, int64_t hi2) {
@@ -428,6 +522,50 @@ int ff_ab3_update(int prec, int64_t n, void* sol, void* RHS, void* RHSm1, void* 
                euler, h1, h2, h3, (const double*)filter),
       LAUNCH1D(k_ab3<float>, n, n, (float2*)sol, (float2*)RHS, (float2*)RHSm1, (float2*)RHSm2, coef<float>(L),
                (float)dt, euler, (float)h1, (float)h2, (float)h3, (const float*)filter));
+  return FF_OK;
+}
+
+int ff_linear_step(int prec, int stepper, int64_t n, void* sol, ff_coef c, double dt, const void* filter,
+                   int64_t nsteps, void* stream) {
+  FF_CHECK_ARG(sol, "ff_linear_step: null state");
+  FF_CHECK_ARG(stepper == FF_STEP_ETDRK4 || stepper == FF_STEP_RK4, "ff_linear_step: ETDRK4 or RK4 only (got %d)",
+               stepper);
+  FF_CHECK_ARG(nsteps >= 0 && nsteps <= (1 << 20), "ff_linear_step: nsteps out of range");
+  FF_CHECK_ARG(c.kind != FF_COEF_NONE, "ff_linear_step: missing coefficient");
+  if (int st = check_coef(c, "ff_linear_step")) return st;
+  if (n <= 0 || nsteps == 0) return FF_OK;
+  auto s = (cudaStream_t)stream;
+  const int ns = (int)nsteps;
+  if (stepper == FF_STEP_ETDRK4) {
+    const bool vec = prec == FF_F32 && c.kind == FF_COEF_REAL && ((uintptr_t)sol % 16) == 0 &&
+                     ((uintptr_t)c.ptr % 8) == 0 && ((uintptr_t)filter % 8) == 0;
+    if (vec) {
+      const int64_t np = n / 2;
+      if (np > 0) {
+        k_linear_etd_f32x2<<<elementwise_grid(np, 256), 256, 0, s>>>(np, (float4*)sol, (const float2*)c.ptr,
+                                                                       (const float2*)filter, ns);
+        FF_LAUNCHED("k_linear_etd_f32x2");
+      }
+      if (n % 2) {  // the last mode of an odd count
+        ff_coef t = c;
+        t.ptr = (const float*)c.ptr + (n - 1);
+        k_linear_etd<float><<<1, 32, 0, s>>>(1, (float2*)sol + (n - 1), coef<float>(t),
+                                             filter ? (const float*)filter + (n - 1) : nullptr, ns);
+        FF_LAUNCHED("k_linear_etd");
+      }
+      return FF_OK;
+    }
+    FF_PREC_DISPATCH(prec,
+        LAUNCH1D(k_linear_etd<double>, n, n, (double2*)sol, coef<double>(c), (const double*)filter, ns),
+        LAUNCH1D(k_linear_etd<float>, n, n, (float2*)sol, coef<float>(c), (const float*)filter, ns));
+    return FF_OK;
+  }
+  // RK4: the stage constants rounded to the state precision as the generic path's are
+  FF_PREC_DISPATCH(prec,
+      LAUNCH1D(k_linear_rk4<double>, n, n, (double2*)sol, coef<double>(c), dt / 2.0, dt, dt / 6.0,
+               (const double*)filter, ns),
+      LAUNCH1D(k_linear_rk4<float>, n, n, (float2*)sol, coef<float>(c), (float)dt / 2.0f, (float)dt,
+               (float)dt / 6.0f, (const float*)filter, ns));
   return FF_OK;
 }
 

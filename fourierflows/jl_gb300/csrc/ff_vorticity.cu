@@ -627,8 +627,16 @@ template <typename T> int profile_t(ff_vort* h, int reps, cudaStream_t s, double
     set_error("ff_vort_profile: only ETDRK4 and RK4 handles can be profiled without advancing the state");
     return FF_ERR_UNSUPPORTED;
   }
-  cudaEvent_t ev[4];
-  for (auto& e : ev) FF_CUDA(cudaEventCreate(&e));
+  // every event created is destroyed on every return path, including FF_CUDA's early ones
+  struct Events {
+    cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+    ~Events() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } guard;
+  cudaEvent_t* ev = guard.e;
+  for (int k = 0; k < 4; ++k) FF_CUDA(cudaEventCreate(&ev[k]));
   double acc[3] = {0, 0, 0};
   int st = FF_OK;
   EpiScalars<T> S{};
@@ -656,7 +664,6 @@ template <typename T> int profile_t(ff_vort* h, int reps, cudaStream_t s, double
       acc[k] += t;
     }
   }
-  for (auto& e : ev) cudaEventDestroy(e);
   for (int k = 0; k < 3; ++k) ms[k] = acc[k] / reps;
   return st;
 }

@@ -48,12 +48,46 @@ class Vars(AbstractVars):
         self.cxh = zeros(dev, cxtype(T), (grid.nkr,))
 
 
+class _LinearStep:
+    """Whole steps of a constant-kappa problem, where calcN! gives N = 0: one native pass
+    per step (``ff_linear_step``) instead of the stepper's four N fills and four substep
+    passes.  ETDRK4 then computes sol = exp(L dt) sol exactly (every N term adds an exact
+    zero); RK4 runs its four linear stages in registers in the generic kernels' order.
+    The stepper's intermediate buffers are not touched.  Falls back to the generic
+    substeps if params.kappa is an array at step time."""
+
+    def __init__(self, ts, eq):
+        from . import timesteppers as tsm
+        self.ts, self.eq = ts, eq
+        self.kind = _lib.FF_STEP_ETDRK4 if isinstance(ts, tsm.ETDRK4TimeStepper) else _lib.FF_STEP_RK4
+
+    def step(self, sol, clock, vars, params, grid):
+        from .timesteppers import _coef, _opt
+        if on_device(params.κ):
+            self.ts._step(sol, clock, self.eq, vars, params, grid)
+            return
+        n = sol.numel()
+        c = self.ts.expLdt if self.kind == _lib.FF_STEP_ETDRK4 else self.eq.L
+        _lib.call("ff_linear_step", prec_of(sol.dtype), self.kind, n, ptr(sol, "sol"), _coef(c, n), float(clock.dt),
+                  _opt(self.ts.filter), 1, stream_handle())
+
+
 class _DiffusionCalcN:
     """calcN!(N, sol, t, clock, vars, params, grid), src/diffusion.jl:129-143.
 
     Constant kappa: N = 0.  Array kappa: cxh = i kr sol; cx = irfft(cxh); cx *= kappa;
     cxh = rfft(cx); N = i kr cxh -- four native launches."""
     __name__ = "calcN!"
+
+    def fused_stepper(self, ts, eq):
+        """A one-pass step for an equation built with constant kappa (N = 0) under the
+        ETDRK4 and RK4 steppers (plain or Filtered), or None for the generic substeps."""
+        from . import timesteppers as tsm
+        if not getattr(eq, "zero_N", False) or not isinstance(eq.grid.device, GPU):
+            return None
+        if isinstance(ts, (tsm.ETDRK4TimeStepper, tsm.RK4TimeStepper)):
+            return _LinearStep(ts, eq)
+        return None
 
     def __call__(self, N, sol, t, clock, vars, params, grid):
         k = params.κ
@@ -78,7 +112,13 @@ def Equation(grid, params):
         return _Equation(0, calcN_, grid, dims=(grid.nkr,), T=cxtype(grid.T))
     kr = grid.kr_host.reshape(-1).astype(np.float64)
     L = (-params.κ * kr ** 2).astype(grid.T)
-    return _Equation(device_array(grid.device)(L), calcN_, grid)
+    return _linear(_Equation(device_array(grid.device)(L), calcN_, grid))
+
+
+def _linear(eq):
+    """Mark an equation whose calcN! is this module's with constant kappa (N = 0)."""
+    eq.zero_N = True
+    return eq
 
 
 def Problem(dev=None, *, nx=128, Lx=2 * math.pi, κ=0, kappa=None, dt=0.01, stepper="RK4", aliased_fraction=0,
@@ -123,14 +163,15 @@ def Problem3D(dev=None, *, n, L=2 * math.pi, kappa, dt, stepper="ETDRK4", T=np.f
     grid = ThreeDGrid(dev, nx=n, Lx=L, aliased_fraction=0, T=T)
     params = Params(kappa)
     Lop = (-kappa * grid.Krsq_host.astype(np.float64)).astype(T)
-    eq = _Equation(device_array(dev)(Lop), calcN_, grid)
+    eq = _linear(_Equation(device_array(dev)(Lop), calcN_, grid))
     return _Problem(eq, stepper, dt, grid, None, params)
 
 
 class Ensemble3D:
     """B independent constant-kappa diffusion problems on one ThreeDGrid n^3, stacked along
     a trailing batch dimension and advanced as one problem: L = -kappa_b Krsq has shape
-    (nkr, n, n, B), so each substep of the stepper is one native pass over all members.
+    (nkr, n, n, B), and with N = 0 each ETDRK4 or RK4 step is one native pass over all
+    members (``ff_linear_step``).
     Initial conditions are Gaussian blobs (width sigma) at counter-based random centres."""
 
     def __init__(self, kappas, n=128, L=2 * math.pi, dt=2e-3, stepper="ETDRK4", T=np.float32, sigma=0.3, seed=7,
@@ -145,7 +186,7 @@ class Ensemble3D:
         Lop = np.empty(g.spectral_shape + (B,), dtype=T, order="F")
         for b in range(B):
             Lop[..., b] = -self.kappas[b] * Krsq
-        eq = _Equation(device_array(dev)(Lop), calcN_, g, dims=Lop.shape)
+        eq = _linear(_Equation(device_array(dev)(Lop), calcN_, g, dims=Lop.shape))
         kw = {"coefficients": "device"} if stepper.replace("Filtered", "") == "ETDRK4" else {}
         self.prob = _Problem(eq, stepper, dt, g, None, Params(0.0), **kw)
         # Gaussian blobs at random centres (minimum-image distance on the periodic box)

@@ -120,6 +120,17 @@ int ff_rk4_update(int prec, int64_t n, void* sol, void* RHS4, ff_coef L, const v
 int ff_lsrk54_stage(int prec, int64_t n, void* sol, void* RHS, void* S2, ff_coef L, double A, double B,
                     double dt, int first, const void* filter, void* stream);
 
+/* nsteps whole steps of a linear equation (N = 0, as the Diffusion module's calcN! gives
+ * for constant kappa, src/diffusion.jl:129-133) in one pass over the state.
+ * stepper FF_STEP_ETDRK4: c = exp(L dt); each step is sol = [filter *] (c sol), which is
+ *   what ETDRK4substeps! + ETDRK4update! (src/timesteppers.jl:501-547,552) compute when
+ *   N1..N4 are zero.
+ * stepper FF_STEP_RK4: c = L; each step runs RK4's four stages with N = 0 in the order of
+ *   ff_rk4_substep / ff_rk4_update (src/timesteppers.jl:225-285), + filter.
+ * The stepper's intermediate buffers (sol1, N1, ...) are neither read nor written. */
+int ff_linear_step(int prec, int stepper, int64_t n, void* sol, ff_coef c, double dt, const void* filter,
+                   int64_t nsteps, void* stream);
+
 /* ETDRK4substep12! (src/timesteppers.jl:506-510): out = e_half sol + zeta N */
 int ff_etdrk4_substep12(int prec, int64_t n, void* out, ff_coef e_half, const void* sol, ff_coef zeta,
                         const void* N, void* stream);
@@ -190,9 +201,11 @@ int ff_radialspectrum(int prec, int is_complex, const void* fh, int64_t n0, int6
  * memory (a pooling allocator that has reserved it, or a fixed-budget embedded code).
  * The caller passes uh and a device double `out` (written on `stream`, no host
  * synchronisation); the scratch is a 32 KiB static device array, so n0 * nrest is limited
- * to 33,554,432 modes (larger sizes return FF_ERR_ARG).  The first call on each device
- * looks up that array's device address; make it before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race. */
+ * to 33,554,432 modes (larger sizes return FF_ERR_ARG).  The first call in each CUDA
+ * context looks up that array's device address (cached by the context's unique ID, so
+ * a device reset or a re-created primary context looks it up again); make that first
+ * call before any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race. */
 int ff_parsevalsum2_noalloc(int prec, const void* uh, int64_t n0, int64_t nrest, int rfft_form, double norm,
                             double* out, void* stream);
 
@@ -245,7 +258,10 @@ int ff_vort_destroy(ff_vort* h);
  * call captures a CUDA graph of one step (set FF_NO_GRAPH=1 to launch kernels directly). */
 int ff_vort_step(ff_vort* h, int64_t nsteps, void* stream);
 
-/* The bare nonlinear term N = calcN!(sol) of problem `prob` (nkr*ny complex each). */
+/* The bare nonlinear term N = calcN!(sol) of problem `prob` (nkr*ny complex each).
+ * Each call stages its descriptor and work lists through one buffer of the handle and
+ * uses the handle's workspace, so calls on one handle must be serialised on one stream
+ * (as ff_vort_step's are); concurrent calls need separate handles. */
 int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream);
 
 /* Average device time (ms) of each of the three passes over `reps` launches, timed with

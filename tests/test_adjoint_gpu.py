@@ -106,3 +106,67 @@ def test_fp32_adjoint_vs_fp64_differences(ff, cuda):
             vals.append(a64.loss(tgt64))
         fd = (vals[0] - vals[1]) / 2e-4
         assert abs(dL - fd) <= 1e-4 * abs(fd), (dL, fd)
+
+
+def test_fp32_adjoint_512_is_the_transpose_of_its_own_map(ff, cuda):
+    """The differentiation form's grid (512^2, nu = 1e-4, mu = 1e-2, dt = 2e-3), FP32 state and
+    adjoint with FP64 reductions.  (1) <J(s)^T lam, d> = <lam, J(s) d> at an FP32 state, the
+    right side from the oracle's FP64 tangent at the same (FP32-rounded) state: 1e-5.
+    (2) One checkpoint segment (50 steps): the FP32 adjoint gradient along a physical
+    direction against the oracle's tangent propagated through the FP32 forward states, with
+    the FP32-rounded ETDRK4 coefficients: 1e-4.  Agreement here, where the FP32 gradient
+    disagrees with FP64 differences by ~1e-2 after 2000 steps, shows that the gap is the
+    FP32 forward map's own drift, not an inexact adjoint."""
+    import os
+    before = orc.WORKERS
+    orc.set_workers(os.cpu_count() or 1)
+    try:
+        _fp32_adjoint_512(ff)
+    finally:
+        orc.set_workers(before)
+
+
+def _fp32_adjoint_512(ff):
+    n, K = 512, 50
+    nu, mu, dt = 1e-4, 1e-2, 2e-3
+    dev = ff.device_array(ff.GPU())
+    p32, a32 = setup(ff, n, nu=nu, mu=mu, dt=dt, T=np.float32, K=K)
+    op = orc.VorticityProblem(n, 2 * math.pi, nu, mu, dt, "ETDRK4")
+    ts = op.timestepper
+    for name in ("expLdt", "exp_half_Ldt", "zeta", "alpha", "beta", "Gamma"):
+        setattr(ts, name, np.asarray(getattr(ts, name)).astype(np.float32).astype(np.float64))
+    g = op.grid
+    rng = np.random.default_rng(31)
+    # (1) the transposed nonlinear term at one FP32 state
+    z = ff.Vorticity.random_phase_vorticity(n, seed=21).astype(np.float32)
+    s32 = ff.rfft(dev(z))
+    s = ff.to_numpy(s32).astype(np.complex128)
+    lam = (rng.standard_normal(s.shape) + 1j * rng.standard_normal(s.shape)).astype(np.complex64)
+    d = rng.standard_normal(s.shape) + 1j * rng.standard_normal(s.shape)
+    out = ff.zeros(ff.GPU(), np.complex64, s.shape)
+    a32._JT(out, s32, dev(lam))
+    lhs = redot(ff.to_numpy(out).astype(np.complex128), d)
+    rhs = redot(lam.astype(np.complex128), orc.vorticity_calcN_tangent(s, d, g))
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    # (2) one 50-step segment
+    z0 = ff.Vorticity.random_phase_vorticity(n, seed=22)
+    zt = ff.Vorticity.random_phase_vorticity(n, seed=23).astype(np.float32)
+    tgt32 = ff.rfft(dev(zt))
+    _, gz, _ = a32.gradient(z0, tgt32, K)
+    fwd = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=2 * math.pi, nu=nu, mu=mu, dt=dt, stepper="ETDRK4", T=np.float32)
+    ff.Vorticity.set_zeta_(fwd, z0)
+    states = [ff.to_numpy(fwd.sol).astype(np.complex128)]
+    for _ in range(K):
+        ff.stepforward_(fwd)
+        states.append(ff.to_numpy(fwd.sol).astype(np.complex128))
+    delta = rng.standard_normal((n, n))
+    ds = orc.rfft(delta.astype(np.float32).astype(np.float64))
+    for k in range(K):
+        _, ds = orc.etdrk4_vorticity_tangent_step(states[k], ds, ts, g)
+    sT, t = states[K], ff.to_numpy(tgt32).astype(np.complex128)
+    w = np.full(sT.shape, 2.0)
+    w[0] = w[-1] = 1.0
+    c1, c2 = 1.0 / (n * n) ** 2, 0.5 / (n * n) ** 2
+    dL_tan = redot(2 * c1 * w * (sT - t) + 2 * c2 * w * sT, ds)
+    dL_adj = float(np.sum(ff.to_numpy(gz).astype(np.float64) * delta.astype(np.float32).astype(np.float64)))
+    assert abs(dL_adj - dL_tan) <= 1e-4 * abs(dL_tan), (dL_adj, dL_tan, abs(dL_adj - dL_tan) / abs(dL_tan))

@@ -74,6 +74,44 @@ def test_diffusion_step_until(ff, cuda, stepper):
     assert abs(float(prob.clock.t) - t_final) < 1e-15
 
 
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredETDRK4", "RK4", "FilteredRK4"])
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_linear_step_matches_generic_substeps(ff, cuda, stepper, T):
+    """Constant kappa (N = 0): the one-pass step (ff_linear_step) gives the generic
+    substeps' bits -- ETDRK4 is exactly exp(L dt) sol, RK4 its four linear stages in the
+    generic kernels' order.  nx = 254 gives an odd mode count (the vectorised FP32 pass
+    then handles the last mode apart)."""
+    x = None
+    out = []
+    for fused in (True, False):
+        p = ff.Diffusion.Problem(ff.GPU(), nx=254, Lx=2 * math.pi, κ=1e-2, dt=0.05, stepper=stepper, T=T)
+        if not fused:
+            p.eqn.zero_N = False
+        x = p.grid.x
+        ff.Diffusion.set_c_(p, np.exp(-x ** 2 / (2 * 0.3 ** 2)) + 0.1 * np.sin(3 * x))
+        assert (p.timestepper._native(p.eqn) is not None) == fused
+        ff.stepforward_(p, 40)
+        out.append(ff.to_numpy(p.sol))
+        assert p.clock.step == 40
+    assert np.array_equal(out[0], out[1])
+
+
+def test_linear_step_3d_ensemble_vs_oracle(ff, cuda):
+    """The stacked 3D constant-kappa ensemble on the one-pass step: every member against
+    its own oracle run (ThreeDGrid, L = -kappa Krsq, N = 0)."""
+    kappas = [1e-3, 4e-3, 1e-2]
+    ens = ff.Diffusion.Ensemble3D(kappas, n=16, dt=2e-3, T=np.float64)
+    assert ens.prob.timestepper._native(ens.prob.eqn) is not None
+    s0 = ff.to_numpy(ens.prob.sol).copy()
+    ens.stepforward_(25)
+    got = ff.to_numpy(ens.prob.sol)
+    for b, kappa in enumerate(kappas):
+        op = orc.Diffusion3DProblem(16, 2 * math.pi, kappa, 2e-3, "ETDRK4")
+        op.sol[...] = s0[..., b]
+        orc.stepforward(op, 25)
+        assert isapprox(got[..., b], op.sol, rtol=1e-13), b
+
+
 def test_diffusion_config_case(ff, cuda):
     """The Diffusion problem on nx=128, Lx=2pi, kappa=1e-2, c0=exp(-x^2/(2 0.3^2)),
     RK4 and ETDRK4 with dt=0.01 for 500 steps: each Fourier mode decays as exp(-kappa k^2 t)."""

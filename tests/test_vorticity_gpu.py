@@ -288,14 +288,19 @@ def test_state_with_aliased_modes(ff, cuda, stepper, T):
 def test_profile_pass_times(ff, cuda):
     """ff_vort_profile on ETDRK4 and RK4 handles (state untouched); an LSRK54 stage would
     advance the state, so that handle is refused."""
-    for stepper, T in (("ETDRK4", np.float64), ("ETDRK4", np.float32), ("RK4", np.float32)):
-        prob, _ = make_pair(ff, 64, stepper, T=T)
+    # 64^2: the register path (FP32: pass C fused with the next pass A); 48^2: the generic
+    # shared-memory path (radix 3), where pass C runs over every column tile unfused
+    cases = [(64, "ETDRK4", np.float64), (64, "ETDRK4", np.float32), (64, "RK4", np.float32),
+             (64, "RK4", np.float64), (48, "ETDRK4", np.float64), (48, "RK4", np.float32)]
+    for n, stepper, T in cases:
+        prob, _ = make_pair(ff, n, stepper, T=T)
         ff.stepforward_(prob, 1)
         fs = prob.timestepper._native(prob.eqn).fs
+        assert (fs.config()["radix_order"] == -1) == (n == 64)
         before = ff.to_numpy(prob.sol)
         ms = fs.profile(reps=2)
-        assert len(ms) == 3 and all(t > 0 for t in ms)
-        assert np.array_equal(ff.to_numpy(prob.sol), before)
+        assert len(ms) == 3 and all(t > 0 for t in ms), (n, stepper, T)
+        assert np.array_equal(ff.to_numpy(prob.sol), before), (n, stepper, T)
     prob, _ = make_pair(ff, 64, "LSRK54")
     ff.stepforward_(prob, 1)
     with pytest.raises(Exception, match="ETDRK4 and RK4"):
