@@ -181,16 +181,16 @@ def survey_step_bytes(n, s):
     return 20 * (C + R) + 21 * C
 
 
-# Per-launch counters from ncu captures (one launch, cold L2; profiles/ holds each summary and
-# the command that made it).  FP64 counts are thread instructions (DFMA = 2 flops); DRAM bytes
+# Per-launch counters from ncu captures (one launch, cold L2; the summaries of these captures,
+# with the commands that made them, are kept with the profiles).  FP64 counts are thread instructions (DFMA = 2 flops); DRAM bytes
 # are read + write and miss the outputs still in L2 when the kernel ends.
 NCU = {
     "fp64_1024": {
-        "capture": "profiles/k_vort_b_fp64_1024.md: ncu --set full, 1024^2 FP64, pass B of step 2",
+        "capture": "ncu --set full on bench.py --profile-case fp64: 1024^2 FP64, k_vort_b_r<double>, step 2",
         "B": {"dadd": 57.30e6, "dmul": 20.21e6, "dfma": 21.13e6, "dram_bytes": 17.45e6},
     },
     "fp32_batch4_1024": {
-        "capture": "profiles/k_vort_passes_fp32_batch4_1024.md: ncu --set full, 4 x 1024^2 FP32, step 2",
+        "capture": "ncu --set full on bench.py --profile-case batch: 4 x 1024^2 FP32, passes B and C of step 2",
         "B": {"dram_bytes": 33.84e6}, "C": {"dram_bytes": 40.90e6},
     },
 }
@@ -462,6 +462,11 @@ def run_forms(torch, ff, a, hbm, peak_src, fused_fp64):
     spec = [(128, nus[i], 1000 + i) for i in range(128)] + [(256, nus[128 + i], 2000 + i) for i in range(128)]
     spec += [(512, nus[256 + i], 3000 + i) for i in range(96)] + [(1024, nus[352 + i], 4000 + i) for i in range(32)]
     ens = ff.Vorticity.Ensemble(spec, mu=MU, dt=DT, T=np.float32)
+    saved = [m.sol.clone() for m in ens.members]
+    ens.fs.autotune(steps_per_trial=1)
+    for m, s in zip(ens.members, saved):
+        m.sol.copy_(s)
+    del saved
     ens.fs.advance(a.warmup)
     msu = timed_steps(torch, ens.fs, bsteps, flush) / bsteps
     gp = ens.grid_points
@@ -469,6 +474,7 @@ def run_forms(torch, ff, a, hbm, peak_src, fused_fp64):
     usurvey = sum(survey_step_bytes(n, 4) for n, _, _ in spec)
     ugbs = ubytes / (msu * 1e-3) / 1e9
     out["ensemble_uneven_384"] = {"value": 384 * 1e3 / msu, "unit": "problem-steps/s", "ms_per_step": msu,
+                                  "tiles": ens.fs.config(),
                                   "grid_point_steps_per_s": gp * 1e3 / msu, "problems": 384,
                                   "sizes": "128x128^2 + 128x256^2 + 96x512^2 + 32x1024^2", "dtype": "f32",
                                   "roofline": {"bound": "hbm", "achieved": ugbs, "peak": hbm, "unit": "GB/s",
@@ -612,6 +618,69 @@ def diffusion3d_ensemble(torch, ff, a, hbm, peak_src, flush):
                     "sol = exp(L dt) sol; the stepper's N fills and substep passes are skipped"}
 
 
+def fp32_adjoint_segment_check(torch, ff, n=512, K=50):
+    """Is the FP32 adjoint the transpose of its own map?  One checkpoint segment (K steps at
+    n^2): the FP32 adjoint's directional derivative against an FP64 tangent-linear sweep
+    along the FP32 forward states, with the FP32-rounded ETDRK4 coefficients.  The tangent
+    of the nonlinear term comes from the library's FP64 calcN! by polarisation: N is
+    bilinear, so J(s) d = (N(s + l d) - N(s) - N(l d)) / l, with l = |s| / |d|."""
+    import numpy as np
+    dev = ff.device_array(ff.GPU())
+    p32 = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=NU, mu=MU, dt=DT, stepper="ETDRK4", T=np.float32)
+    a32 = ff.Adjoint.VorticityAdjoint(p32, checkpoint_every=K)
+    z0 = ff.Vorticity.random_phase_vorticity(n, seed=SEED + 22)
+    zt = ff.Vorticity.random_phase_vorticity(n, seed=SEED + 23).astype(np.float32)
+    tgt = ff.rfft(dev(zt))
+    _, gz, _ = a32.gradient(z0, tgt, K)
+    # the FP32 forward states of the segment
+    ff.Vorticity.set_zeta_(p32, z0)
+    states = [p32.sol.clone()]
+    for _ in range(K):
+        ff.stepforward_(p32)
+        states.append(p32.sol.clone())
+    p64 = ff.Vorticity.Problem(ff.GPU(), nx=n, Lx=LX, nu=NU, mu=MU, dt=DT, stepper="ETDRK4")
+    ts = p32.timestepper
+    E, E2, Z, A, B, G = (c.double() for c in (ts.expLdt, ts.exp_half_Ldt, ts.zeta, ts.alpha, ts.beta, ts.Gamma))
+
+    def N(x):
+        out = torch.empty_like(x)
+        ff.Vorticity.calcN_(out, x, 0.0, p64.clock, p64.vars, p64.params, p64.grid)
+        return out
+
+    def J(x, d):
+        lam = float(torch.linalg.vector_norm(x) / torch.linalg.vector_norm(d))
+        return (N(x + lam * d) - N(x) - N(lam * d)) / lam
+
+    delta = np.random.default_rng(SEED + 24).standard_normal((n, n)).astype(np.float32)
+    ds = ff.rfft(dev(delta.astype(np.float64)))
+    for k in range(K):
+        s = states[k].to(torch.complex128)
+        N1 = N(s)
+        a = E2 * s + Z * N1
+        N2 = N(a)
+        b = E2 * s + Z * N2
+        N3 = N(b)
+        c = E2 * a + Z * (2 * N3 - N1)
+        dN1 = J(s, ds)
+        da = E2 * ds + Z * dN1
+        dN2 = J(a, da)
+        db = E2 * ds + Z * dN2
+        dN3 = J(b, db)
+        dc = E2 * da + Z * (2 * dN3 - dN1)
+        dN4 = J(c, dc)
+        ds = E * ds + A * dN1 + 2 * B * (dN2 + dN3) + G * dN4
+    sT, t = states[K].to(torch.complex128), tgt.to(torch.complex128)
+    w = torch.full(sT.shape, 2.0, dtype=torch.float64, device=sT.device)
+    w[0] = 1.0
+    w[-1] = 1.0
+    c1, c2 = 1.0 / (n * n) ** 2, 0.5 / (n * n) ** 2
+    g = 2 * c1 * w * (sT - t) + 2 * c2 * w * sT
+    dL_tan = float(torch.sum((torch.conj(g) * ds).real))
+    dL_adj = float(np.sum(ff.to_numpy(gz).astype(np.float64) * delta.astype(np.float64)))
+    return {"steps": K, "grid": f"{n}^2", "dL_adjoint_fp32": dL_adj, "dL_tangent_fp64_on_fp32_states": dL_tan,
+            "rel_err": abs(dL_adj - dL_tan) / abs(dL_tan)}
+
+
 def adjoint_512(torch, ff, ndir=8, nsteps=2000):
     """Discrete adjoint of 512^2 ETDRK4 (dt 2e-3, 2000 steps, checkpoint every 50): FP32
     forward and adjoint with FP64 gradient reductions; loss = mean((zeta_T - zeta_target)^2)
@@ -671,6 +740,8 @@ def adjoint_512(torch, ff, ndir=8, nsteps=2000):
                      "adjoint_steps_per_s": nsteps / res[name]["seconds"],
                      "max_rel_err_vs_fp64_fd": {f"h={h:g}": v for h, v in worst[name].items()}}
     out["nu_rel_err_vs_fp64_fd"] = nu_rel
+    # the FP32 adjoint against a tangent of its own map over one checkpoint segment
+    out["fp32"]["segment_vs_tangent_of_fp32_map"] = fp32_adjoint_segment_check(torch, ff)
     # what bounds the FP32 figures: the FP32 forward map itself drifts from the FP64 one
     g32, g64 = res["fp32"]["grad"], res["fp64"]["grad"]
     f32, f64 = res["fp32"]["final"], res["fp64"]["final"]

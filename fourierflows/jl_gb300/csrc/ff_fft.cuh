@@ -92,6 +92,75 @@ template <typename T, int DIR> struct Dft<T, 8, DIR> {
   }
 };
 
+// FP32 butterflies on Blackwell's packed FP32 instructions.  A float2 complex value is one
+// register pair and FADD2 / FFMA2 / FMUL2 apply one operation to both halves, so an
+// untwiddled complex add or subtract is one instruction instead of two.  A product with
+// +-i swaps the halves; it is folded into an FFMA2 with a sign pair (x*1 + a and x*-1 + a
+// round exactly as a + x and a - x do), so every result is the scalar form's, bit for bit.
+#ifndef FF_PACKED_F32
+#define FF_PACKED_F32 1
+#endif
+#if FF_PACKED_F32  // sm_100 and later (this library builds for sm_103a only)
+namespace pk {
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 swp(float2 a) { return make_float2(a.y, a.x); }
+// a + rot<DIR>(b) and a - rot<DIR>(b); rot is -i (DIR < 0: (b.y, -b.x)) or +i ((-b.y, b.x))
+template <int DIR> __device__ __forceinline__ float2 add_rot(float2 a, float2 b) {
+  return __ffma2_rn(swp(b), DIR < 0 ? make_float2(1.f, -1.f) : make_float2(-1.f, 1.f), a);
+}
+template <int DIR> __device__ __forceinline__ float2 sub_rot(float2 a, float2 b) {
+  return __ffma2_rn(swp(b), DIR < 0 ? make_float2(-1.f, 1.f) : make_float2(1.f, -1.f), a);
+}
+}  // namespace pk
+
+template <int DIR> struct Dft<float, 2, DIR> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float2 a = v[0], b = v[1];
+    v[0] = pk::add(a, b);
+    v[1] = pk::sub(a, b);
+  }
+};
+
+// v[2] enters multiplied by rot<DIR> when rot2 (the radix-8 butterfly's b[2] * W8^2)
+template <int DIR, bool ROT2 = false> __device__ __forceinline__ void dft4_packed(float2* v) {
+  const float2 s02 = ROT2 ? pk::add_rot<DIR>(v[0], v[2]) : pk::add(v[0], v[2]);
+  const float2 d02 = ROT2 ? pk::sub_rot<DIR>(v[0], v[2]) : pk::sub(v[0], v[2]);
+  const float2 s13 = pk::add(v[1], v[3]);
+  const float2 x = pk::sub(v[1], v[3]);  // d13 = rot<DIR>(x)
+  v[0] = pk::add(s02, s13);
+  v[2] = pk::sub(s02, s13);
+  v[1] = pk::add_rot<DIR>(d02, x);
+  v[3] = pk::sub_rot<DIR>(d02, x);
+}
+
+template <int DIR> struct Dft<float, 4, DIR> {
+  static __device__ __forceinline__ void run(float2* v) { dft4_packed<DIR>(v); }
+};
+
+template <int DIR> struct Dft<float, 8, DIR> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float h = float(FF_SQRT1_2);
+    float2 a[4], b[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      a[r] = pk::add(v[r], v[r + 4]);
+      b[r] = pk::sub(v[r], v[r + 4]);
+    }
+    // b[1] *= W8 = (1 -+ i)/sqrt2: (b + rot(b)) h; b[3] *= W8^3 = -(1 +- i)/sqrt2: (b + rot'(b)) (-h)
+    b[1] = __fmul2_rn(pk::add_rot<DIR>(b[1], b[1]), make_float2(h, h));
+    b[3] = __fmul2_rn(pk::add_rot<-DIR>(b[3], b[3]), make_float2(-h, -h));
+    dft4_packed<DIR>(a);
+    dft4_packed<DIR, true>(b);  // b[2] *= W8^2 = rot<DIR>, folded into its first adds
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      v[2 * q] = a[q];
+      v[2 * q + 1] = b[q];
+    }
+  }
+};
+#endif
+
 template <typename T, int DIR> struct Dft<T, 3, DIR> {
   static __device__ __forceinline__ void run(cx<T>* v) {
     const T s = T(FF_SQRT3_2);

@@ -12,6 +12,7 @@
 //   fft   : rows C2C (in -> out), cols y, cols z (in place)
 //   ifft  : the same with the inverse direction, the last pass scaled by 1/N.
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -255,10 +256,16 @@ __global__ void k_cols(const cx<T>* in, cx<T>* out, int64_t ncols, int n, int64_
 // ---------------------------------------------------------------------------------------
 template <typename T> static int prec_of() { return sizeof(T) == 8 ? FF_F64 : FF_F32; }
 
+bool plan_generic_forced() {
+  const char* e = getenv("FF_PLAN_GENERIC");
+  return e && e[0] == '1';
+}
+
 template <typename T>
 int launch_r2c_rows(const T* in, cx<T>* out, int64_t nrows, int nx, const LinePlan& P, const cx<T>* tw,
                     const cx<T>* rtw, cudaStream_t s) {
   if (nrows <= 0) return FF_OK;
+  if (reg_rows_ok(nx / 2) && !plan_generic_forced()) return launch_r2c_rows_reg<T>(in, out, nrows, nx, tw, rtw, s);
   const RowGeom g = row_geom(nx / 2, prec_of<T>());
   int st = ensure_smem((const void*)k_r2c_rows<T>, g.smem);
   if (st) return st;
@@ -271,6 +278,8 @@ template <typename T>
 int launch_c2r_rows(const cx<T>* in, T* out, int64_t nrows, int nx, const LinePlan& P, const cx<T>* tw,
                     const cx<T>* rtw, T scale, cudaStream_t s) {
   if (nrows <= 0) return FF_OK;
+  if (reg_rows_ok(nx / 2) && !plan_generic_forced())
+    return launch_c2r_rows_reg<T>(in, out, nrows, nx, tw, rtw, scale, s);
   const RowGeom g = row_geom(nx / 2, prec_of<T>());
   int st = ensure_smem((const void*)k_c2r_rows<T>, g.smem);
   if (st) return st;
@@ -284,6 +293,7 @@ template <typename T, int DIR>
 int launch_c2c_rows(const cx<T>* in, cx<T>* out, int64_t nrows, int n, const LinePlan& P, const cx<T>* tw,
                     T scale, cudaStream_t s) {
   if (nrows <= 0) return FF_OK;
+  if (reg_line_ok(n) && !plan_generic_forced()) return launch_c2c_rows_reg<T, DIR>(in, out, nrows, n, tw, scale, s);
   const RowGeom g = row_geom(n, prec_of<T>());
   // row_geom sizes for a line of length n here (not n/2)
   int st = ensure_smem((const void*)k_c2c_rows<T, DIR>, g.smem);
@@ -298,6 +308,8 @@ template <typename T, int DIR>
 int launch_cols(const cx<T>* in, cx<T>* out, int64_t ncols, int n, int64_t stride, int64_t nouter,
                 int64_t outer_stride, const LinePlan& P, const cx<T>* tw, T scale, cudaStream_t s) {
   if (ncols <= 0 || nouter <= 0) return FF_OK;
+  if (reg_line_ok(n) && !plan_generic_forced())
+    return launch_cols_reg<T, DIR>(in, out, ncols, n, stride, nouter, outer_stride, tw, scale, s);
   const ColGeom g = col_geom(n, prec_of<T>());
   int st = ensure_smem((const void*)k_cols<T, DIR>, g.smem);
   if (st) return st;

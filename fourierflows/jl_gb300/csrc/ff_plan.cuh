@@ -49,4 +49,23 @@ template <typename T, int DIR>
 int launch_cols(const cx<T>* in, cx<T>* out, int64_t ncols, int n, int64_t stride, int64_t nouter,
                 int64_t outer_stride, const LinePlan& P, const cx<T>* tw, T scale, cudaStream_t s);
 
+// Register-resident passes for power-of-two lengths (ff_plan_reg.cu): rows of nx/2 <= 2048
+// complex values, lines of n <= 4096.  The launchers above route to them when the length
+// qualifies, unless FF_PLAN_GENERIC=1.
+bool reg_rows_ok(int h);
+bool reg_line_ok(int n);
+bool plan_generic_forced();
+template <typename T>
+int launch_r2c_rows_reg(const T* in, cx<T>* out, int64_t nrows, int nx, const cx<T>* tw, const cx<T>* rtw,
+                        cudaStream_t s);
+template <typename T>
+int launch_c2r_rows_reg(const cx<T>* in, T* out, int64_t nrows, int nx, const cx<T>* tw, const cx<T>* rtw, T scale,
+                        cudaStream_t s);
+template <typename T, int DIR>
+int launch_c2c_rows_reg(const cx<T>* in, cx<T>* out, int64_t nrows, int n, const cx<T>* tw, T scale,
+                        cudaStream_t s);
+template <typename T, int DIR>
+int launch_cols_reg(const cx<T>* in, cx<T>* out, int64_t ncols, int n, int64_t stride, int64_t nouter,
+                    int64_t outer_stride, const cx<T>* tw, T scale, cudaStream_t s);
+
 }  // namespace ff

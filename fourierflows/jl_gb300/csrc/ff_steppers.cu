@@ -343,19 +343,35 @@ __device__ __forceinline__ double block_sum(double v) {
 }
 
 // mode 0: |u|^2 [* wt]; mode 1: Re u.  rfft_form weights rows 1..n0-2 by 2.
+// On GB300 FP64 runs at 2 instructions per SM per cycle, so with FP64 data this reduction
+// is bound by the FP64 pipe before HBM: each mode costs two FMAs into one of two
+// accumulators (rows counted once, rows counted twice; the factor 2 is applied once at the
+// end), one more with a weight.  The row index i0 = i mod n0 advances by S mod n0 (S = the
+// grid's thread count) instead of a 64-bit division per mode.
+template <typename T>
+__device__ __forceinline__ void parseval_add(const cx<T>* __restrict__ uh, const T* __restrict__ wt, int64_t i,
+                                             bool twice, int mode, double& a1, double& a2) {
+  const cx<T> u = uh[i];
+  const double x = (double)u.x, y = (double)u.y;
+  double& a = twice ? a2 : a1;
+  if (mode != 0) a += x;
+  else if (wt) a = fma(fma(x, x, y * y), (double)wt[i], a);
+  else a = fma(y, y, fma(x, x, a));
+}
+
 template <typename T>
 __global__ void k_parseval_partial(const cx<T>* __restrict__ uh, int64_t n0, int64_t total, int rfft_form, int mode,
                                    const T* __restrict__ wt, double* partial) {
-  double acc = 0.0;
-  GRID_STRIDE(i, total) {
-    const cx<T> u = uh[i];
-    double v = mode == 0 ? (double)u.x * (double)u.x + (double)u.y * (double)u.y : (double)u.x;
-    if (wt) v *= (double)wt[i];
-    const int64_t i0 = i % n0;
-    const double w = (rfft_form && i0 > 0 && i0 < n0 - 1) ? 2.0 : 1.0;
-    acc += w * v;
+  const int64_t S = (int64_t)gridDim.x * blockDim.x, s0 = S % n0;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t i0 = i % n0;
+  double a1 = 0.0, a2 = 0.0;
+  for (; i < total; i += S) {
+    parseval_add(uh, wt, i, rfft_form && i0 > 0 && i0 < n0 - 1, mode, a1, a2);
+    i0 += s0;
+    if (i0 >= n0) i0 -= n0;
   }
-  acc = block_sum(acc);
+  const double acc = block_sum(a1 + 2.0 * a2);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 

@@ -13,6 +13,7 @@ struct PassLaunch {
   int tile;   // generic path: tile width / rows per CTA
   bool reg;   // register-resident power-of-two kernels
   bool fuse = false;  // pass C, register path: also the next substep's pass A
+  int stage_off = 0, stage_sz = 0;  // pass B, register path: shared-memory input stages (bytes)
 };
 
 struct EpiArgs {  // precision-independent copy of EpiScalars
@@ -32,7 +33,7 @@ int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const void* w
 
 // kernel entry points (for occupancy queries and shared-memory limits)
 template <typename T> const void* vort_kernel_a(bool reg);
-template <typename T> const void* vort_kernel_b(bool reg);
+template <typename T> const void* vort_kernel_b(bool reg, bool staged = false);
 template <typename T> const void* vort_kernel_c(bool reg, int epi, bool fuse = false);
 
 constexpr int kNumEpilogues = 10;

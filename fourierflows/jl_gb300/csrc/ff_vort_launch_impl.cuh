@@ -33,8 +33,18 @@ int vort_launch_a(const PassLaunch& L, const void* probs, const void* work, int 
 template <typename T>
 int vort_launch_b(const PassLaunch& L, const void* probs, const void* work, int nwork, cudaStream_t s) {
   const auto* P = (const VortProb<T>*)probs;
-  if (L.reg) k_vort_b_r<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork);
-  else k_vort_b<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.tile);
+  bool done = false;
+  if constexpr (sizeof(T) == 4) {  // FP64 pass B never stages
+    if (L.reg && L.stage_sz > 0) {
+      k_vort_b_r<T, true><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.stage_off,
+                                                            L.stage_sz);
+      done = true;
+    }
+  }
+  if (!done) {
+    if (L.reg) k_vort_b_r<T, false><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, 0, 0);
+    else k_vort_b<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.tile);
+  }
   FF_LAUNCHED("k_vort_b");
   return FF_OK;
 }
@@ -76,8 +86,12 @@ int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const void* w
 template <typename T> const void* vort_kernel_a(bool reg) {
   return reg ? (const void*)k_vort_a_r<T> : (const void*)k_vort_a<T>;
 }
-template <typename T> const void* vort_kernel_b(bool reg) {
-  return reg ? (const void*)k_vort_b_r<T> : (const void*)k_vort_b<T>;
+template <typename T> const void* vort_kernel_b(bool reg, bool staged) {
+  if (!reg) return (const void*)k_vort_b<T>;
+  if constexpr (sizeof(T) == 4) {
+    if (staged) return (const void*)k_vort_b_r<T, true>;
+  }
+  return (const void*)k_vort_b_r<T, false>;
 }
 template <typename T, int EPI> static const void* fuse_ptr(bool fuse) {
   if constexpr (EPI != EPI_N && EPI != EPI_ETD4 && EPI != EPI_RK4) {
@@ -103,7 +117,7 @@ template <typename T> const void* vort_kernel_c(bool reg, int epi, bool fuse) {
   template int vort_launch_c<T>(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&,           \
                                 cudaStream_t);                                                                   \
   template const void* vort_kernel_a<T>(bool);                                                                   \
-  template const void* vort_kernel_b<T>(bool);                                                                   \
+  template const void* vort_kernel_b<T>(bool, bool);                                                             \
   template const void* vort_kernel_c<T>(bool, int, bool);
 
 }  // namespace ff

@@ -23,6 +23,7 @@ struct Geom {
   int ga = 0, gb = 0, gc = 0;      // grid sizes
   int radix_variant = 0;           // generic path: 0 radix-8 first, 1 radix-4 first, 2 small radix first
   bool reg = false;                // register-resident power-of-two kernels
+  int b_stage_off = 0, b_stage_sz = 0;  // register pass B: shared-memory input stages (0: direct loads)
 };
 
 int pow2_floor(int v) {
@@ -109,7 +110,24 @@ static int64_t wq_pitch(int64_t nkd, size_t es) {
   return (nkd + m - 1) / m * m;
 }
 
-template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, int tlr) {
+// Register pass B in FP32 can stage its input rows through shared memory (cp.async, one
+// item ahead) instead of loading them directly: the autotuner tries both (variant 1 flips
+// the default, direct loads), since the stages' shared memory costs occupancy when a CTA
+// holds many short rows; FF_VORT_B_STAGE=0/1 forces either.  FP64 pass B is bound by the
+// FP64 pipe and always loads directly.
+#ifndef FF_B_STAGED_F32
+#define FF_B_STAGED_F32 0
+#endif
+
+template <typename T> bool b_staged(int variant) {
+  if (sizeof(T) == 8) return false;  // FP64 pass B is FP64-pipe bound: direct loads only
+  const char* e = getenv("FF_VORT_B_STAGE");
+  if (e && (e[0] == '0' || e[0] == '1')) return e[0] == '1';
+  const bool dflt = FF_B_STAGED_F32 != 0;
+  return variant == 1 ? !dflt : dflt;
+}
+
+template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, int tlr, int variant) {
   Geom g;
   g.reg = true;
   const size_t es = elem<T>();
@@ -142,11 +160,24 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
     smb = std::max(smb, 3 * rows * (size_t)(H + (H >> sh) + 1) * es);
   }
   g.smb = smb;
+  if (b_staged<T>(variant)) {
+    size_t ssz = 0;
+    for (const auto& q : h->host) {
+      const size_t rows = (size_t)g.thb * 8 / (size_t)(q.nx / 2);
+      ssz = std::max(ssz, 3 * rows * (size_t)wq_pitch(q.nkd, es) * es);
+    }
+    const size_t off = (smb + 15) / 16 * 16;
+    ssz = (ssz + 15) / 16 * 16;
+    g.b_stage_off = (int)off;
+    g.b_stage_sz = (int)ssz;
+    g.smb = off + 2 * ssz;
+  }
+  g.radix_variant = variant;
   return g;
 }
 
 template <typename T> Geom choose_geom(const ff_vort* h, int tla, int tlc, int tlr, int variant) {
-  if (reg_capable(h)) return choose_geom_reg<T>(h, tla, tlc, tlr);
+  if (reg_capable(h)) return choose_geom_reg<T>(h, tla, tlc, tlr, variant);
   Geom g;
   const int ny = h->max_ny, hx = h->max_nx / 2;
   const size_t es = elem<T>();
@@ -265,7 +296,15 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
     return (int64_t)probs[a.prob].nx * probs[a.prob].ny > (int64_t)probs[b.prob].nx * probs[b.prob].ny;
   };
   std::stable_sort(wa.begin(), wa.end(), by_size);
-  std::stable_sort(wb.begin(), wb.end(), by_size);
+  // Pass B walks problems of equal size in the reverse order of passes A and C, so that
+  // it starts on the problems whose W the column pass wrote last (still in L2 when an
+  // ensemble's W is larger than L2), and pass C starts on the Q that B wrote last.
+  auto by_size_rev = [&](const WorkItem& a, const WorkItem& b) {
+    const int64_t sa = (int64_t)probs[a.prob].nx * probs[a.prob].ny, sb = (int64_t)probs[b.prob].nx * probs[b.prob].ny;
+    if (sa != sb) return sa > sb;
+    return a.prob > b.prob;
+  };
+  std::stable_sort(wb.begin(), wb.end(), by_size_rev);
   // pass C: tiles of kept columns first (largest problems first), then aliased columns
   auto kept_then_size = [&](const WorkItem& a, const WorkItem& b) {
     const int wa_c = geom.reg ? geom.thc * 8 / probs[a.prob].ny : geom.tlc;
@@ -312,7 +351,7 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   FF_CUDA(cudaMemcpy(h->d_inputs, in.data(), sizeof(void*) * in.size(), cudaMemcpyHostToDevice));
   h->g = geom;
   const void* ka = vort_kernel_a<T>(geom.reg);
-  const void* kb = vort_kernel_b<T>(geom.reg);
+  const void* kb = vort_kernel_b<T>(geom.reg, geom.b_stage_sz > 0);
   if (int st = ensure_smem(ka, geom.sma)) return st;
   if (int st = ensure_smem(kb, geom.smb)) return st;
   for (int e = 0; e < kNumEpilogues; ++e)
@@ -337,7 +376,10 @@ int launch_a(const ff_vort* h, const void* probs, const void* work, int nwork, i
 
 template <typename T>
 int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, cudaStream_t s) {
-  return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg}, probs, work, nwork, s);
+  PassLaunch L{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg};
+  L.stage_off = h->g.b_stage_off;
+  L.stage_sz = h->g.b_stage_sz;
+  return vort_launch_b<T>(L, probs, work, nwork, s);
 }
 
 template <typename T, int EPI>
@@ -553,7 +595,8 @@ int ff_vort_config(const ff_vort* h, int32_t cfg[8]) {
   cfg[0] = h->g.tla;
   cfg[1] = h->g.tlc;
   cfg[2] = h->g.tlr;
-  cfg[3] = h->g.reg ? -1 : h->g.radix_variant;  // -1: register-resident power-of-two path
+  // -1: register-resident power-of-two path; -2: the same with pass B staged through shared memory
+  cfg[3] = h->g.reg ? (h->g.b_stage_sz > 0 ? -2 : -1) : h->g.radix_variant;
   cfg[4] = h->g.tha;
   cfg[5] = h->g.thb;
   cfg[6] = h->g.thc;
@@ -575,8 +618,9 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   const int reps = steps_per_trial > 0 ? steps_per_trial : 3;
   const int tls_f64[] = {1, 2, 4, 8};
   const int tls_f32[] = {1, 2, 4, 8};
-  // the register path has one stage schedule; only the generic path varies radix order
-  const int nvar = reg_capable(h) ? 1 : 3;
+  // the generic path varies the radix order; the register path has one stage schedule and
+  // varies whether pass B stages its inputs through shared memory
+  const int nvar = reg_capable(h) ? 2 : 3;
   const int* tls = h->prec == FF_F64 ? tls_f64 : tls_f32;
   const int ntl = 4;
   double best = 1e30;

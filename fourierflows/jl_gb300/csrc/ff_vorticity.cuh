@@ -537,8 +537,11 @@ __device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __
 
 // Loads go straight from W (an L2 prefetch one item ahead, see k_vort_b_r) into
 // registers; shared memory holds only the exchanges.
-template <typename T, int H>
-__device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>* smem) {
+// STAGED: the rows come from `stage`, the shared-memory copy of this item's rows (field f,
+// row ln at (f * rows + ln) * nkp); otherwise straight from W
+template <typename T, int H, bool STAGED>
+__device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>* smem,
+                                           const cx<T>* __restrict__ stage) {
   constexpr int PP = H / 8;
   constexpr int SH = sizeof(T) == 8 ? 3 : 4;
   constexpr int STRIDE = H + (H >> SH) + 1;
@@ -547,10 +550,12 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   const int j = tile * rows + ln;
   const int ny = P.ny, nkd = P.nkd, nkp = P.nkp;
   const int fstride = nkp * ny;
+  const cx<T>* xbase = STAGED ? stage + ln * nkp : P.W + j * nkp;
+  const int xfs = STAGED ? rows * nkp : fstride;
   cx<T> v[3][8];
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
-    const cx<T>* src = P.W + f * fstride + j * nkp;
+    const cx<T>* src = xbase + f * xfs;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = t + q * PP;
@@ -818,29 +823,81 @@ template <typename T> __device__ __forceinline__ void prefetch_b(const VortProb<
     prefetch_lines(P.W + f * fstride + j0 * P.nkp, nr * P.nkp, threadIdx.x, blockDim.x);
 }
 
-// Pass B, persistent over row blocks; each item's rows are prefetched into L2 one item
-// ahead.  (A pipeline of bulk copies into shared memory with mbarrier waits measured
-// 5% slower in FP32 and 9% in FP64 at 1024^2 than these direct loads.)
-template <typename T>
+// 16-byte asynchronous copies global -> shared (no registers held, no completion to poll:
+// cp.async.wait_group returns when this thread's older groups have landed)
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// every 16-byte chunk of item it's three W row blocks into `stage` (field f, row r at
+// (f * rows + r) * nkp; nkp complex values are a whole number of chunks)
+template <typename T> __device__ __forceinline__ void stage_b(const VortProb<T>& P, const WorkItem& it, cx<T>* stage) {
+  const int rows = blockDim.x * 8 / (P.nx / 2), j0 = it.tile * rows;
+  const int nr = min(rows, P.ny - j0);
+  if (nr <= 0) return;
+  constexpr int E = 16 / (int)sizeof(cx<T>);  // complex values per chunk
+  const int nkp = P.nkp, cpr = nkp / E;
+  const int64_t fstride = (int64_t)nkp * P.ny;
+  const int total = 3 * nr * cpr;
+  for (int c = threadIdx.x; c < total; c += blockDim.x) {
+    const int fr = c / cpr, k = (c - fr * cpr) * E;
+    const int f = fr / nr, r = fr - f * nr;
+    cp_async16(stage + (f * rows + r) * nkp + k, P.W + f * fstride + (int64_t)(j0 + r) * nkp + k);
+  }
+}
+
+// Pass B, persistent over row blocks.  STAGED: each item's W rows are copied into one of
+// two shared-memory stages (at byte offsets stage_off and stage_off + stage_sz) while the
+// previous item is transformed, so the transforms read their inputs from shared memory.
+// Otherwise direct loads, with the next item's rows prefetched into L2.
+template <typename T, bool STAGED>
 __global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restrict__ probs,
-                                                  const WorkItem* __restrict__ work, int nwork) {
+                                                  const WorkItem* __restrict__ work, int nwork, int stage_off,
+                                                  int stage_sz) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  cx<T>* const stage0 = reinterpret_cast<cx<T>*>(smem_raw + stage_off);
+  cx<T>* const stage1 = reinterpret_cast<cx<T>*>(smem_raw + stage_off + stage_sz);
+  if (STAGED) {
+    if ((int)blockIdx.x < nwork) {
+      const WorkItem it0 = work[blockIdx.x];
+      stage_b(probs[it0.prob], it0, stage0);
+    }
+    cp_async_commit();
+  }
+  int i = 0;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x, ++i) {
     const WorkItem it = work[w];
     const VortProb<T>& P = probs[it.prob];
-    if (w + (int)gridDim.x < nwork) {
-      const WorkItem nxt = work[w + gridDim.x];
+    const int wn = w + (int)gridDim.x;
+    if (STAGED) {
+      // the stage written here was last read by the item before, which ended with a barrier
+      if (wn < nwork) {
+        const WorkItem nxt = work[wn];
+        stage_b(probs[nxt.prob], nxt, (i & 1) ? stage0 : stage1);
+      }
+      cp_async_commit();
+      cp_async_wait<1>();  // this item's copies (every group but the newest) have landed
+      __syncthreads();
+    } else if (wn < nwork) {
+      const WorkItem nxt = work[wn];
       prefetch_b(probs[nxt.prob], nxt);
     }
+    const cx<T>* st = (i & 1) ? stage1 : stage0;
     switch (P.nx / 2) {
 #define FF_B_CASE(N) \
-  case N: vort_b_reg<T, N>(P, it.tile, smem); break;
+  case N: vort_b_reg<T, N, STAGED>(P, it.tile, smem, st); break;
       FF_REG_CASES_B(FF_B_CASE)
 #undef FF_B_CASE
       default: break;
     }
   }
+  if (STAGED) cp_async_wait<0>();
 }
 
 template <typename T, int EPI, bool FUSE>

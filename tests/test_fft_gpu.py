@@ -216,3 +216,31 @@ def test_plan_errors(ff, cuda):
     dev = ff.device_array(ff.GPU())
     with pytest.raises(ValueError):
         ff.mul_(ff.zeros(ff.GPU(), np.complex128, (9,)), plan, dev(np.zeros(12)))
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("n", [(64,), (4096,), (32, 64), (512, 256), (16, 4096), (2048, 16), (16, 32, 8)])
+def test_register_and_generic_plan_kernels_agree(ff, cuda, monkeypatch, prec, n):
+    """Power-of-two lengths run the register-resident plan kernels (ff_plan_reg.cu);
+    FF_PLAN_GENERIC=1 sends the same plans through the shared-memory Stockham kernels.
+    rfft, irfft, fft and ifft agree between the two paths and with the oracle."""
+    T = np.float64 if prec == "f64" else np.float32
+    tol = 1e-12 if prec == "f64" else 2e-6
+    rng = np.random.default_rng(sum(n))
+    x = rng.standard_normal(n).astype(T)
+    z = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex128 if prec == "f64" else np.complex64)
+    dev = ff.device_array(ff.GPU())
+    res = {}
+    for path in ("register", "generic"):
+        monkeypatch.setenv("FF_PLAN_GENERIC", "1" if path == "generic" else "0")
+        xh = ff.rfft(dev(x))
+        back = ff.irfft(xh, n[0])
+        zh = ff.fft(dev(z))
+        zb = ff.ifft(zh)
+        res[path] = [ff.to_numpy(a) for a in (xh, back, zh, zb)]
+    want = [orc.rfft(x.astype(np.float64)), x.astype(np.float64), orc.fft(z.astype(np.complex128)),
+            z.astype(np.complex128)]
+    for a, b, w in zip(res["register"], res["generic"], want):
+        a, b = a.astype(w.dtype), b.astype(w.dtype)
+        assert isapprox(a, b, rtol=tol), (n, prec)
+        assert isapprox(a, w, rtol=tol), (n, prec)

@@ -79,12 +79,12 @@ def test_diffusion_step_until(ff, cuda, stepper):
 def test_linear_step_matches_generic_substeps(ff, cuda, stepper, T):
     """Constant kappa (N = 0): the one-pass step (ff_linear_step) gives the generic
     substeps' bits -- ETDRK4 is exactly exp(L dt) sol, RK4 its four linear stages in the
-    generic kernels' order.  nx = 254 gives an odd mode count (the vectorised FP32 pass
-    then handles the last mode apart)."""
+    generic kernels' order.  nx = 252 gives an odd mode count (nkr = 127: the vectorised
+    FP32 pass handles the last mode apart); dt kappa kr_max^2 = 1.6 keeps RK4 stable."""
     x = None
     out = []
     for fused in (True, False):
-        p = ff.Diffusion.Problem(ff.GPU(), nx=254, Lx=2 * math.pi, κ=1e-2, dt=0.05, stepper=stepper, T=T)
+        p = ff.Diffusion.Problem(ff.GPU(), nx=252, Lx=2 * math.pi, κ=1e-2, dt=0.01, stepper=stepper, T=T)
         if not fused:
             p.eqn.zero_N = False
         x = p.grid.x
@@ -93,6 +93,7 @@ def test_linear_step_matches_generic_substeps(ff, cuda, stepper, T):
         ff.stepforward_(p, 40)
         out.append(ff.to_numpy(p.sol))
         assert p.clock.step == 40
+    assert np.all(np.isfinite(out[0]))
     assert np.array_equal(out[0], out[1])
 
 
