@@ -154,7 +154,8 @@ def pass_bytes(n, es, fused_a, filtered=False):
            (nkd columns x lrows rows); substep 4 also advances the aliased modes by
            exp(L dt) alone (sol and exp(L dt) in, sol out).  fused_a (FP32): pass C of
            substeps 1-3 also runs the next substep's pass A (kept 1/K^2 in, W out), so A
-           runs apart only in substep 1."""
+           runs apart only in substep 1, and the intermediate states sol1 / sol2 pass to it
+           in registers instead of through HBM (substep 3 rebuilds sol1 from sol and N1)."""
     from fourierflows.jl_gb300.domains import getaliasedwavenumbers
     nkr = n // 2 + 1
     lal, kral = getaliasedwavenumbers(n, nkr, 1 / 3)
@@ -165,8 +166,11 @@ def pass_bytes(n, es, fused_a, filtered=False):
     a_in, a_out = K * (es + rs), 3 * Wd
     b = 5 * Wd
     fl = rs if filtered else 0
-    epi = {1: K * (3 * es + 2 * rs), 2: K * (3 * es + 2 * rs), 3: K * (4 * es + 2 * rs),
-           4: K * (5 * es + 4 * rs + fl) + (M - K) * (2 * es + rs + fl)}
+    if fused_a:  # sol (+ N1) and e_half, zeta in; N_k out
+        epi = {1: K * (2 * es + 2 * rs), 2: K * (2 * es + 2 * rs), 3: K * (3 * es + 2 * rs)}
+    else:        # the input state (+ N1) and e_half, zeta in; N_k and the next state out
+        epi = {1: K * (3 * es + 2 * rs), 2: K * (3 * es + 2 * rs), 3: K * (4 * es + 2 * rs)}
+    epi[4] = K * (5 * es + 4 * rs + fl) + (M - K) * (2 * es + rs + fl)
     c = {k: 2 * Wd + epi[k] + ((K * rs + a_out) if fused_a and k < 4 else 0) for k in (1, 2, 3, 4)}
     step = (a_in + a_out) * (1 if fused_a else 4) + 4 * b + sum(c.values())
     return {"A": a_in + a_out, "B": b, "C1": c[1], "C2": c[2], "C3": c[3], "C4": c[4], "step": step}

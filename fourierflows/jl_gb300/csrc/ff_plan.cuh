@@ -50,8 +50,9 @@ int launch_cols(const cx<T>* in, cx<T>* out, int64_t ncols, int n, int64_t strid
                 int64_t outer_stride, const LinePlan& P, const cx<T>* tw, T scale, cudaStream_t s);
 
 // Register-resident passes for power-of-two lengths (ff_plan_reg.cu): rows of nx/2 <= 2048
-// complex values, lines of n <= 4096.  The launchers above route to them when the length
-// qualifies, unless FF_PLAN_GENERIC=1.
+// complex values (FP32 real transforms), lines of n <= 4096 (complex rows and columns, both
+// precisions).  The launchers above route to them when the length qualifies, unless
+// FF_PLAN_GENERIC=1.
 bool reg_rows_ok(int h);
 bool reg_line_ok(int n);
 bool plan_generic_forced();

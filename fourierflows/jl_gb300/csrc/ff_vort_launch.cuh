@@ -26,15 +26,36 @@ int vort_launch_a(const PassLaunch& L, const void* probs, const void* work, int 
                   cudaStream_t s);
 template <typename T>
 int vort_launch_b(const PassLaunch& L, const void* probs, const void* work, int nwork, cudaStream_t s);
-// epi: one of the Epilogue values of ff_vorticity.cuh
+// epi: one of the Epilogue values of ff_vorticity.cuh (0..4: bare calcN! and ETDRK4,
+// 5..9: RK4 and LSRK54); each family is instantiated in its own translation unit
+int vort_launch_c_etd_f32(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&, cudaStream_t);
+int vort_launch_c_rk_f32(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&, cudaStream_t);
+int vort_launch_c_etd_f64(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&, cudaStream_t);
+int vort_launch_c_rk_f64(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&, cudaStream_t);
+const void* vort_kernel_c_etd_f32(bool reg, int epi, bool fuse);
+const void* vort_kernel_c_rk_f32(bool reg, int epi, bool fuse);
+const void* vort_kernel_c_etd_f64(bool reg, int epi, bool fuse);
+const void* vort_kernel_c_rk_f64(bool reg, int epi, bool fuse);
+
 template <typename T>
-int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork, const EpiArgs& S,
-                  cudaStream_t s);
+inline int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork,
+                         const EpiArgs& S, cudaStream_t s) {
+  const bool etd = epi <= 4;
+  if (sizeof(T) == 8)
+    return etd ? vort_launch_c_etd_f64(L, epi, probs, work, nwork, S, s)
+               : vort_launch_c_rk_f64(L, epi, probs, work, nwork, S, s);
+  return etd ? vort_launch_c_etd_f32(L, epi, probs, work, nwork, S, s)
+             : vort_launch_c_rk_f32(L, epi, probs, work, nwork, S, s);
+}
 
 // kernel entry points (for occupancy queries and shared-memory limits)
 template <typename T> const void* vort_kernel_a(bool reg);
 template <typename T> const void* vort_kernel_b(bool reg, bool staged = false);
-template <typename T> const void* vort_kernel_c(bool reg, int epi, bool fuse = false);
+template <typename T> inline const void* vort_kernel_c(bool reg, int epi, bool fuse = false) {
+  const bool etd = epi <= 4;
+  if (sizeof(T) == 8) return etd ? vort_kernel_c_etd_f64(reg, epi, fuse) : vort_kernel_c_rk_f64(reg, epi, fuse);
+  return etd ? vort_kernel_c_etd_f32(reg, epi, fuse) : vort_kernel_c_rk_f32(reg, epi, fuse);
+}
 
 constexpr int kNumEpilogues = 10;
 

@@ -1,6 +1,6 @@
-// Fused vorticity kernels instantiated for FP64.
+// Fused vorticity kernels instantiated for FP64: passes A and B.
 #include "ff_vort_launch_impl.cuh"
 
 namespace ff {
-FF_INSTANTIATE_VORT_LAUNCH(double)
+FF_INSTANTIATE_VORT_LAUNCH_AB(double)
 }  // namespace ff

@@ -65,22 +65,50 @@ static void launch_c_epi(const PassLaunch& L, const VortProb<T>* P, const WorkIt
   }
 }
 
+// pass C launchers of one family of epilogues (compiled in their own translation units):
+// ETD = the bare calcN! and the ETDRK4 substeps, RK = the RK4 substeps and the LSRK54 stage
 template <typename T>
-int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork, const EpiArgs& a,
-                  cudaStream_t s) {
+int vort_launch_c_family(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork,
+                         const EpiArgs& a, cudaStream_t s) {
   const auto* P = (const VortProb<T>*)probs;
   const auto* w = (const WorkItem*)work;
   const EpiScalars<T> S = to_scalars<T>(a);
   switch (epi) {
 #define FF_EPI_CASE(E) \
   case E: launch_c_epi<T, E>(L, P, w, nwork, S, s); break;
+#if FF_C_FAMILY_ETD
     FF_EPI_CASE(EPI_N) FF_EPI_CASE(EPI_ETD1) FF_EPI_CASE(EPI_ETD2) FF_EPI_CASE(EPI_ETD3) FF_EPI_CASE(EPI_ETD4)
+#endif
+#if FF_C_FAMILY_RK
     FF_EPI_CASE(EPI_RK1) FF_EPI_CASE(EPI_RK2) FF_EPI_CASE(EPI_RK3) FF_EPI_CASE(EPI_RK4) FF_EPI_CASE(EPI_LS)
+#endif
 #undef FF_EPI_CASE
-    default: set_error("vort_launch_c: bad epilogue %d", epi); return FF_ERR_ARG;
+    default: set_error("vort_launch_c: epilogue %d is not in this family", epi); return FF_ERR_ARG;
   }
   FF_LAUNCHED("k_vort_c");
   return FF_OK;
+}
+
+template <typename T, int EPI> static const void* fuse_ptr(bool fuse) {
+  if constexpr (EPI != EPI_N && EPI != EPI_ETD4 && EPI != EPI_RK4) {
+    if (fuse) return (const void*)k_vort_c_r<T, EPI, true>;
+  }
+  return (const void*)k_vort_c_r<T, EPI, false>;
+}
+
+template <typename T> const void* vort_kernel_c_family(bool reg, int epi, bool fuse) {
+  switch (epi) {
+#define FF_EPI_PTR(E) \
+  case E: return !reg ? (const void*)k_vort_c<T, E> : fuse_ptr<T, E>(fuse);
+#if FF_C_FAMILY_ETD
+    FF_EPI_PTR(EPI_N) FF_EPI_PTR(EPI_ETD1) FF_EPI_PTR(EPI_ETD2) FF_EPI_PTR(EPI_ETD3) FF_EPI_PTR(EPI_ETD4)
+#endif
+#if FF_C_FAMILY_RK
+    FF_EPI_PTR(EPI_RK1) FF_EPI_PTR(EPI_RK2) FF_EPI_PTR(EPI_RK3) FF_EPI_PTR(EPI_RK4) FF_EPI_PTR(EPI_LS)
+#endif
+#undef FF_EPI_PTR
+    default: return nullptr;
+  }
 }
 
 template <typename T> const void* vort_kernel_a(bool reg) {
@@ -93,31 +121,18 @@ template <typename T> const void* vort_kernel_b(bool reg, bool staged) {
   }
   return (const void*)k_vort_b_r<T, false>;
 }
-template <typename T, int EPI> static const void* fuse_ptr(bool fuse) {
-  if constexpr (EPI != EPI_N && EPI != EPI_ETD4 && EPI != EPI_RK4) {
-    if (fuse) return (const void*)k_vort_c_r<T, EPI, true>;
-  }
-  return (const void*)k_vort_c_r<T, EPI, false>;
-}
 
-template <typename T> const void* vort_kernel_c(bool reg, int epi, bool fuse) {
-  switch (epi) {
-#define FF_EPI_PTR(E) \
-  case E: return !reg ? (const void*)k_vort_c<T, E> : fuse_ptr<T, E>(fuse);
-    FF_EPI_PTR(EPI_N) FF_EPI_PTR(EPI_ETD1) FF_EPI_PTR(EPI_ETD2) FF_EPI_PTR(EPI_ETD3) FF_EPI_PTR(EPI_ETD4)
-    FF_EPI_PTR(EPI_RK1) FF_EPI_PTR(EPI_RK2) FF_EPI_PTR(EPI_RK3) FF_EPI_PTR(EPI_RK4) FF_EPI_PTR(EPI_LS)
-#undef FF_EPI_PTR
-    default: return nullptr;
-  }
-}
-
-#define FF_INSTANTIATE_VORT_LAUNCH(T)                                                                            \
+// passes A and B, and pass C, in separate translation units (they compile in parallel)
+#define FF_INSTANTIATE_VORT_LAUNCH_AB(T)                                                                         \
   template int vort_launch_a<T>(const PassLaunch&, const void*, const void*, int, const void*, cudaStream_t);    \
   template int vort_launch_b<T>(const PassLaunch&, const void*, const void*, int, cudaStream_t);                 \
-  template int vort_launch_c<T>(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&,           \
-                                cudaStream_t);                                                                   \
   template const void* vort_kernel_a<T>(bool);                                                                   \
-  template const void* vort_kernel_b<T>(bool, bool);                                                             \
-  template const void* vort_kernel_c<T>(bool, int, bool);
+  template const void* vort_kernel_b<T>(bool, bool);
+#define FF_INSTANTIATE_VORT_LAUNCH_C(T, NAME)                                                                    \
+  int vort_launch_c_##NAME(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork,          \
+                           const EpiArgs& a, cudaStream_t s) {                                                   \
+    return vort_launch_c_family<T>(L, epi, probs, work, nwork, a, s);                                            \
+  }                                                                                                              \
+  const void* vort_kernel_c_##NAME(bool reg, int epi, bool fuse) { return vort_kernel_c_family<T>(reg, epi, fuse); }
 
 }  // namespace ff

@@ -282,8 +282,11 @@ template <typename T> struct EpiIn {
 };
 
 // live: false on the aliased l rows of kept columns under ETDRK4, where N is zero and the
-// intermediates are never read: only what the last substep's expL sol [f] needs is loaded
-template <typename T, int EPI>
+// intermediates are never read: only what the last substep's expL sol [f] needs is loaded.
+// FUSED (ETDRK4 with pass C running the next substep's pass A): the intermediate states
+// go to the next pass A in registers, so sol1 and sol2 are never stored; substep 3 rebuilds
+// sol1 = e_half sol + zeta n1 from sol and n1, the same operands substep 1 combined.
+template <typename T, int EPI, bool FUSED = false>
 __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e,
                                              bool live = true) {
   EpiIn<T> in;
@@ -302,7 +305,7 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
     in.a = P.eh[e];
     in.b = P.zc[e];
   } else if (EPI == EPI_ETD3) {
-    in.x = P.s1[e];
+    in.x = FUSED ? P.sol[e] : P.s1[e];
     in.n1 = P.n1[e];
     in.a = P.eh[e];
     in.b = P.zc[e];
@@ -336,7 +339,7 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
 
 // the same arithmetic, in the same order, as epilogue<T, EPI>; returns the value stored
 // to the array the next substep transforms (s1, s2 or sol; zero for the last substeps)
-template <typename T, int EPI>
+template <typename T, int EPI, bool FUSED = false>
 __device__ __forceinline__ cx<T> epi_store(const VortProb<T>& P, const EpiScalars<T>& S, int64_t e, cx<T> N,
                                            const EpiIn<T>& in, bool live = true) {
   cx<T> next = czero<T>();
@@ -364,11 +367,12 @@ __device__ __forceinline__ cx<T> epi_store(const VortProb<T>& P, const EpiScalar
   } else if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
     (EPI == EPI_ETD1 ? P.n1 : P.n2)[e] = N;
     next = add(scl(in.x, in.a), scl(N, in.b));
-    (EPI == EPI_ETD1 ? P.s1 : P.s2)[e] = next;
+    if (!FUSED) (EPI == EPI_ETD1 ? P.s1 : P.s2)[e] = next;
   } else if (EPI == EPI_ETD3) {
     P.n3[e] = N;
-    next = add(scl(in.x, in.a), scl(sub(scl(N, T(2)), in.n1), in.b));
-    P.s2[e] = next;
+    const cx<T> x1 = FUSED ? add(scl(in.x, in.a), scl(in.n1, in.b)) : in.x;  // sol1
+    next = add(scl(x1, in.a), scl(sub(scl(N, T(2)), in.n1), in.b));
+    if (!FUSED) P.s2[e] = next;
   } else if (EPI == EPI_ETD4) {
     cx<T> v = add(scl(in.x, in.a), scl(in.n1, in.b));
     v = add(v, scl(scl(add(in.n2, in.n3), in.c), T(2)));
@@ -622,7 +626,7 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
 // Under ETDRK4 and RK4 the aliased modes (c >= nkd or an aliased l row) are "dead": N is
 // zero there, the substeps' intermediates are never read there, and the last substep
 // advances them by the linear part alone.
-template <typename T, int NY, int EPI>
+template <typename T, int NY, int EPI, bool FUSED = false>
 __device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScalars<T>& S, int c, int t,
                                              const cx<T> (&N)[8], cx<T> (&next)[8]) {
   const bool col_live = c < P.nkd;
@@ -633,12 +637,12 @@ __device__ __forceinline__ void epilogue_col(const VortProb<T>& P, const EpiScal
 #pragma unroll
     for (int b = 0; b < QB; ++b) {
       const int j = t + (q0 + b) * PP;
-      in[b] = epi_load<T, EPI>(P, S, c + (int64_t)j * P.nkr, col_live && (j < P.la || j >= P.lb));
+      in[b] = epi_load<T, EPI, FUSED>(P, S, c + (int64_t)j * P.nkr, col_live && (j < P.la || j >= P.lb));
     }
 #pragma unroll
     for (int b = 0; b < QB; ++b) {
       const int j = t + (q0 + b) * PP;
-      next[q0 + b] = epi_store<T, EPI>(P, S, c + (int64_t)j * P.nkr, N[q0 + b], in[b],
+      next[q0 + b] = epi_store<T, EPI, FUSED>(P, S, c + (int64_t)j * P.nkr, N[q0 + b], in[b],
                                        col_live && (j < P.la || j >= P.lb));
     }
   }
@@ -731,7 +735,9 @@ __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalar
       v[0][q] = N;
       v[1][q] = czero<T>();
     }
-    if (c < nkr) epilogue_col<T, NY, EPI>(P, S, c, t, v[0], v[1]);
+    // ETDRK4 substeps 1-3 with the next pass A fused: sol1 / sol2 stay in registers
+    constexpr bool kFusedEtd = FUSE && (EPI == EPI_ETD1 || EPI == EPI_ETD2 || EPI == EPI_ETD3);
+    if (c < nkr) epilogue_col<T, NY, EPI, kFusedEtd>(P, S, c, t, v[0], v[1]);
     if (FUSE) a_from_regs<T, NY>(P, c, t, tl, ln, v[1], smem);
   } else if (c < nkr) {
     // aliased kr columns (substeps 1-3 of ETDRK4 and RK4 do not visit these tiles: their
