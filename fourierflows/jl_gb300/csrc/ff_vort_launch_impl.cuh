@@ -34,8 +34,11 @@ template <typename T>
 int vort_launch_b(const PassLaunch& L, const void* probs, const void* work, int nwork, cudaStream_t s) {
   const auto* P = (const VortProb<T>*)probs;
   bool done = false;
-  if constexpr (sizeof(T) == 4) {  // FP64 pass B never stages
-    if (L.reg && L.stage_sz > 0) {
+  if constexpr (sizeof(T) == 4) {  // FP64 pass B never stages and has no lean form
+    if (L.reg && L.lean) {
+      k_vort_b_r_lean<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork);
+      done = true;
+    } else if (L.reg && L.stage_sz > 0) {
       k_vort_b_r<T, true><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.stage_off,
                                                             L.stage_sz);
       done = true;
@@ -114,9 +117,10 @@ template <typename T> const void* vort_kernel_c_family(bool reg, int epi, bool f
 template <typename T> const void* vort_kernel_a(bool reg) {
   return reg ? (const void*)k_vort_a_r<T> : (const void*)k_vort_a<T>;
 }
-template <typename T> const void* vort_kernel_b(bool reg, bool staged) {
+template <typename T> const void* vort_kernel_b(bool reg, bool staged, bool lean) {
   if (!reg) return (const void*)k_vort_b<T>;
   if constexpr (sizeof(T) == 4) {
+    if (lean) return (const void*)k_vort_b_r_lean<T>;
     if (staged) return (const void*)k_vort_b_r<T, true>;
   }
   return (const void*)k_vort_b_r<T, false>;
@@ -127,7 +131,7 @@ template <typename T> const void* vort_kernel_b(bool reg, bool staged) {
   template int vort_launch_a<T>(const PassLaunch&, const void*, const void*, int, const void*, cudaStream_t);    \
   template int vort_launch_b<T>(const PassLaunch&, const void*, const void*, int, cudaStream_t);                 \
   template const void* vort_kernel_a<T>(bool);                                                                   \
-  template const void* vort_kernel_b<T>(bool, bool);
+  template const void* vort_kernel_b<T>(bool, bool, bool);
 #define FF_INSTANTIATE_VORT_LAUNCH_C(T, NAME)                                                                    \
   int vort_launch_c_##NAME(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork,          \
                            const EpiArgs& a, cudaStream_t s) {                                                   \

@@ -24,6 +24,7 @@ struct Geom {
   int radix_variant = 0;           // generic path: 0 radix-8 first, 1 radix-4 first, 2 small radix first
   bool reg = false;                // register-resident power-of-two kernels
   int b_stage_off = 0, b_stage_sz = 0;  // register pass B: shared-memory input stages (0: direct loads)
+  bool b_lean = false;                   // register pass B (FP32): one field besides zeta at a time
 };
 
 int pow2_floor(int v) {
@@ -160,7 +161,11 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
     smb = std::max(smb, 3 * rows * (size_t)(H + (H >> sh) + 1) * es);
   }
   g.smb = smb;
-  if (b_staged<T>(variant)) {
+  if (sizeof(T) == 4 && variant == 2) {
+    // lean pass B: one field's exchange buffer
+    g.b_lean = true;
+    g.smb = smb / 3;
+  } else if (b_staged<T>(variant)) {
     size_t ssz = 0;
     for (const auto& q : h->host) {
       const size_t rows = (size_t)g.thb * 8 / (size_t)(q.nx / 2);
@@ -351,7 +356,7 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   FF_CUDA(cudaMemcpy(h->d_inputs, in.data(), sizeof(void*) * in.size(), cudaMemcpyHostToDevice));
   h->g = geom;
   const void* ka = vort_kernel_a<T>(geom.reg);
-  const void* kb = vort_kernel_b<T>(geom.reg, geom.b_stage_sz > 0);
+  const void* kb = vort_kernel_b<T>(geom.reg, geom.b_stage_sz > 0, geom.b_lean);
   if (int st = ensure_smem(ka, geom.sma)) return st;
   if (int st = ensure_smem(kb, geom.smb)) return st;
   for (int e = 0; e < kNumEpilogues; ++e)
@@ -379,6 +384,7 @@ int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, i
   PassLaunch L{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg};
   L.stage_off = h->g.b_stage_off;
   L.stage_sz = h->g.b_stage_sz;
+  L.lean = h->g.b_lean;
   return vort_launch_b<T>(L, probs, work, nwork, s);
 }
 
@@ -595,8 +601,9 @@ int ff_vort_config(const ff_vort* h, int32_t cfg[8]) {
   cfg[0] = h->g.tla;
   cfg[1] = h->g.tlc;
   cfg[2] = h->g.tlr;
-  // -1: register-resident power-of-two path; -2: the same with pass B staged through shared memory
-  cfg[3] = h->g.reg ? (h->g.b_stage_sz > 0 ? -2 : -1) : h->g.radix_variant;
+  // -1: register-resident power-of-two path; -2: the same with pass B staged through shared
+  // memory; -3: the same with the lean pass B
+  cfg[3] = h->g.reg ? (h->g.b_lean ? -3 : (h->g.b_stage_sz > 0 ? -2 : -1)) : h->g.radix_variant;
   cfg[4] = h->g.tha;
   cfg[5] = h->g.thb;
   cfg[6] = h->g.thc;
@@ -619,8 +626,8 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   const int tls_f64[] = {1, 2, 4, 8};
   const int tls_f32[] = {1, 2, 4, 8};
   // the generic path varies the radix order; the register path has one stage schedule and
-  // varies whether pass B stages its inputs through shared memory
-  const int nvar = reg_capable(h) ? 2 : 3;
+  // varies pass B (direct loads, inputs staged through shared memory, the lean form)
+  const int nvar = 3;
   const int* tls = h->prec == FF_F64 ? tls_f64 : tls_f32;
   const int ntl = 4;
   double best = 1e30;

@@ -621,6 +621,72 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   __syncthreads();
 }
 
+// Pass B with one transformed field in registers besides zeta: C2R of zeta, then for u and
+// v in turn C2R, the product with zeta and R2C.  Each field goes through the same
+// operations as in vort_b_reg (bit-identical results) with a third of the registers held
+// across the transforms, so more rows are in flight per SM (FP32).
+template <typename T, int H>
+__device__ __forceinline__ void vort_b_reg_lean(const VortProb<T>& P, int tile, cx<T>* smem) {
+  constexpr int PP = H / 8;
+  constexpr int SH = sizeof(T) == 8 ? 3 : 4;
+  constexpr int STRIDE = H + (H >> SH) + 1;
+  const int rows = blockDim.x / PP;
+  const int ln = threadIdx.x / PP, t = threadIdx.x & (PP - 1);
+  const int j = tile * rows + ln;
+  const int ny = P.ny, nkd = P.nkd, nkp = P.nkp;
+  const int fstride = nkp * ny;
+  const XRow xr{ln * STRIDE, SH};
+  cx<T>* const buf[1] = {smem};
+  auto load = [&](int f, cx<T>(&v)[1][8]) {
+    const cx<T>* src = P.W + f * fstride + j * nkp;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = t + q * PP;
+      cx<T> val = czero<T>();
+      if (j < ny) {
+        const cx<T> xk = k < nkd ? src[k] : czero<T>();
+        const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
+        val = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]), k);
+      }
+      v[0][q] = val;
+    }
+  };
+  cx<T> z[1][8];
+  load(2, z);
+  regfft<T, 1, H, 1>(z, t, P.twx, buf, xr);
+  const T s2 = P.scale2;
+#pragma unroll 1
+  for (int f = 0; f < 2; ++f) {
+    cx<T> v[1][8];
+    load(f, v);
+    regfft<T, 1, H, 1>(v, t, P.twx, buf, xr);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[0][q] = mk<T>(v[0][q].x * z[0][q].x * s2, v[0][q].y * z[0][q].y * s2);
+    regfft<T, 1, H, -1>(v, t, P.twx, buf, xr);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) smem[xr(t + q * PP)] = v[0][q];
+    __syncthreads();
+    if (j < ny) {
+      cx<T>* qf = P.Q + f * fstride + j * nkp;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = t + q * PP;
+        if (k >= nkd) continue;
+        cx<T> x, dummy;
+        if (k == 0) {
+          const cx<T> z0 = v[0][0];
+          x = mk<T>(z0.x + z0.y, T(0));
+          if (nkd > H) qf[H] = mk<T>(z0.x - z0.y, T(0));  // no dealiasing: the Nyquist column too
+        } else {
+          r2c_pair<T>(v[0][q], smem[xr(H - k)], __ldg(&P.rtw[k]), x, dummy);
+        }
+        qf[k] = x;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // epilogue of thread t's eight elements (rows t + q NY/8) of column c: the loads of a
 // batch of elements first, then their arithmetic and stores
 // Under ETDRK4 and RK4 the aliased modes (c >= nkd or an aliased l row) are "dead": N is
@@ -904,6 +970,30 @@ __global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restr
     }
   }
   if (STAGED) cp_async_wait<0>();
+}
+
+// Pass B, lean form (vort_b_reg_lean): three CTAs of FF_LB_B_THREADS per SM bound the
+// registers (85 per thread), so 64-thread CTAs hold up to 24 warps per SM
+template <typename T>
+__global__ void __launch_bounds__(FF_LB_B_THREADS, 3) k_vort_b_r_lean(const VortProb<T>* __restrict__ probs,
+                                                                    const WorkItem* __restrict__ work, int nwork) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    if (w + (int)gridDim.x < nwork) {
+      const WorkItem nxt = work[w + gridDim.x];
+      prefetch_b(probs[nxt.prob], nxt);
+    }
+    switch (P.nx / 2) {
+#define FF_B_CASE(N) \
+  case N: vort_b_reg_lean<T, N>(P, it.tile, smem); break;
+      FF_REG_CASES_B(FF_B_CASE)
+#undef FF_B_CASE
+      default: break;
+    }
+  }
 }
 
 template <typename T, int EPI, bool FUSE>

@@ -311,17 +311,18 @@ def test_profile_pass_times(ff, cuda):
 @pytest.mark.parametrize("rows_b", [1, 4])
 def test_pass_b_staging_is_bit_identical(ff, cuda, T, rows_b):
     """FP32 register pass B reading its input rows through two shared-memory stages filled
-    one item ahead (cp.async), or straight from W, computes the same bits.  An uneven
-    ensemble puts rows of different lengths in the same stages.  FP64 pass B always loads
-    directly (both variants are the same kernel)."""
+    one item ahead (cp.async), straight from W, or in the lean form (one field besides zeta
+    at a time) computes the same bits.  An uneven ensemble puts rows of different lengths
+    in the same stages.  FP64 pass B always takes the default (the variants are one kernel)."""
     spec = [(256, 1e-3, 1), (64, 3e-4, 2), (128, 1e-4, 3), (256, 2e-4, 4), (32, 5e-4, 5)]
     outs, modes = [], []
-    for variant in (0, 1):
+    for variant in (0, 1, 2):
         ens = ff.Vorticity.Ensemble(spec, mu=1e-2, dt=2e-3, T=T)
         ens.fs.set_config(0, 0, rows_b, variant)
         modes.append(ens.fs.config()["radix_order"])
         ens.stepforward_(5)
         outs.append([ff.to_numpy(m.sol) for m in ens.members])
-    assert sorted(modes) == ([-2, -1] if T == np.float32 else [-1, -1])
-    for a, b in zip(*outs):
-        assert np.array_equal(a, b)
+    assert sorted(modes) == ([-3, -2, -1] if T == np.float32 else [-1, -1, -1])
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
