@@ -13,8 +13,6 @@ struct PassLaunch {
   int tile;   // generic path: tile width / rows per CTA
   bool reg;   // register-resident power-of-two kernels
   bool fuse = false;  // pass C, register path: also the next substep's pass A
-  int stage_off = 0, stage_sz = 0;  // pass B, register path: shared-memory input stages (bytes)
-  bool lean = false;  // pass B, register path (FP32): one field besides zeta in registers at a time
 };
 
 struct EpiArgs {  // precision-independent copy of EpiScalars
@@ -51,7 +49,7 @@ inline int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const 
 
 // kernel entry points (for occupancy queries and shared-memory limits)
 template <typename T> const void* vort_kernel_a(bool reg);
-template <typename T> const void* vort_kernel_b(bool reg, bool staged = false, bool lean = false);
+template <typename T> const void* vort_kernel_b(bool reg);
 template <typename T> inline const void* vort_kernel_c(bool reg, int epi, bool fuse = false) {
   const bool etd = epi <= 4;
   if (sizeof(T) == 8) return etd ? vort_kernel_c_etd_f64(reg, epi, fuse) : vort_kernel_c_rk_f64(reg, epi, fuse);

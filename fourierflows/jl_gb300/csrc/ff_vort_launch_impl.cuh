@@ -33,21 +33,8 @@ int vort_launch_a(const PassLaunch& L, const void* probs, const void* work, int 
 template <typename T>
 int vort_launch_b(const PassLaunch& L, const void* probs, const void* work, int nwork, cudaStream_t s) {
   const auto* P = (const VortProb<T>*)probs;
-  bool done = false;
-  if constexpr (sizeof(T) == 4) {  // FP64 pass B never stages and has no lean form
-    if (L.reg && L.lean) {
-      k_vort_b_r_lean<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork);
-      done = true;
-    } else if (L.reg && L.stage_sz > 0) {
-      k_vort_b_r<T, true><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.stage_off,
-                                                            L.stage_sz);
-      done = true;
-    }
-  }
-  if (!done) {
-    if (L.reg) k_vort_b_r<T, false><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, 0, 0);
-    else k_vort_b<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.tile);
-  }
+  if (L.reg) k_vort_b_r<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork);
+  else k_vort_b<T><<<L.grid, L.threads, L.smem, s>>>(P, (const WorkItem*)work, nwork, L.tile);
   FF_LAUNCHED("k_vort_b");
   return FF_OK;
 }
@@ -117,13 +104,8 @@ template <typename T> const void* vort_kernel_c_family(bool reg, int epi, bool f
 template <typename T> const void* vort_kernel_a(bool reg) {
   return reg ? (const void*)k_vort_a_r<T> : (const void*)k_vort_a<T>;
 }
-template <typename T> const void* vort_kernel_b(bool reg, bool staged, bool lean) {
-  if (!reg) return (const void*)k_vort_b<T>;
-  if constexpr (sizeof(T) == 4) {
-    if (lean) return (const void*)k_vort_b_r_lean<T>;
-    if (staged) return (const void*)k_vort_b_r<T, true>;
-  }
-  return (const void*)k_vort_b_r<T, false>;
+template <typename T> const void* vort_kernel_b(bool reg) {
+  return reg ? (const void*)k_vort_b_r<T> : (const void*)k_vort_b<T>;
 }
 
 // passes A and B, and pass C, in separate translation units (they compile in parallel)
@@ -131,7 +113,7 @@ template <typename T> const void* vort_kernel_b(bool reg, bool staged, bool lean
   template int vort_launch_a<T>(const PassLaunch&, const void*, const void*, int, const void*, cudaStream_t);    \
   template int vort_launch_b<T>(const PassLaunch&, const void*, const void*, int, cudaStream_t);                 \
   template const void* vort_kernel_a<T>(bool);                                                                   \
-  template const void* vort_kernel_b<T>(bool, bool, bool);
+  template const void* vort_kernel_b<T>(bool);
 #define FF_INSTANTIATE_VORT_LAUNCH_C(T, NAME)                                                                    \
   int vort_launch_c_##NAME(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork,          \
                            const EpiArgs& a, cudaStream_t s) {                                                   \

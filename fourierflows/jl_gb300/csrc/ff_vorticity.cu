@@ -23,8 +23,6 @@ struct Geom {
   int ga = 0, gb = 0, gc = 0;      // grid sizes
   int radix_variant = 0;           // generic path: 0 radix-8 first, 1 radix-4 first, 2 small radix first
   bool reg = false;                // register-resident power-of-two kernels
-  int b_stage_off = 0, b_stage_sz = 0;  // register pass B: shared-memory input stages (0: direct loads)
-  bool b_lean = false;                   // register pass B (FP32): one field besides zeta at a time
 };
 
 int pow2_floor(int v) {
@@ -111,24 +109,7 @@ static int64_t wq_pitch(int64_t nkd, size_t es) {
   return (nkd + m - 1) / m * m;
 }
 
-// Register pass B in FP32 can stage its input rows through shared memory (cp.async, one
-// item ahead) instead of loading them directly: the autotuner tries both (variant 1 flips
-// the default, direct loads), since the stages' shared memory costs occupancy when a CTA
-// holds many short rows; FF_VORT_B_STAGE=0/1 forces either.  FP64 pass B is bound by the
-// FP64 pipe and always loads directly.
-#ifndef FF_B_STAGED_F32
-#define FF_B_STAGED_F32 0
-#endif
-
-template <typename T> bool b_staged(int variant) {
-  if (sizeof(T) == 8) return false;  // FP64 pass B is FP64-pipe bound: direct loads only
-  const char* e = getenv("FF_VORT_B_STAGE");
-  if (e && (e[0] == '0' || e[0] == '1')) return e[0] == '1';
-  const bool dflt = FF_B_STAGED_F32 != 0;
-  return variant == 1 ? !dflt : dflt;
-}
-
-template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, int tlr, int variant) {
+template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, int tlr) {
   Geom g;
   g.reg = true;
   const size_t es = elem<T>();
@@ -161,28 +142,11 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
     smb = std::max(smb, 3 * rows * (size_t)(H + (H >> sh) + 1) * es);
   }
   g.smb = smb;
-  if (sizeof(T) == 4 && variant == 2) {
-    // lean pass B: one field's exchange buffer
-    g.b_lean = true;
-    g.smb = smb / 3;
-  } else if (b_staged<T>(variant)) {
-    size_t ssz = 0;
-    for (const auto& q : h->host) {
-      const size_t rows = (size_t)g.thb * 8 / (size_t)(q.nx / 2);
-      ssz = std::max(ssz, 3 * rows * (size_t)wq_pitch(q.nkd, es) * es);
-    }
-    const size_t off = (smb + 15) / 16 * 16;
-    ssz = (ssz + 15) / 16 * 16;
-    g.b_stage_off = (int)off;
-    g.b_stage_sz = (int)ssz;
-    g.smb = off + 2 * ssz;
-  }
-  g.radix_variant = variant;
   return g;
 }
 
 template <typename T> Geom choose_geom(const ff_vort* h, int tla, int tlc, int tlr, int variant) {
-  if (reg_capable(h)) return choose_geom_reg<T>(h, tla, tlc, tlr, variant);
+  if (reg_capable(h)) return choose_geom_reg<T>(h, tla, tlc, tlr);
   Geom g;
   const int ny = h->max_ny, hx = h->max_nx / 2;
   const size_t es = elem<T>();
@@ -356,7 +320,7 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   FF_CUDA(cudaMemcpy(h->d_inputs, in.data(), sizeof(void*) * in.size(), cudaMemcpyHostToDevice));
   h->g = geom;
   const void* ka = vort_kernel_a<T>(geom.reg);
-  const void* kb = vort_kernel_b<T>(geom.reg, geom.b_stage_sz > 0, geom.b_lean);
+  const void* kb = vort_kernel_b<T>(geom.reg);
   if (int st = ensure_smem(ka, geom.sma)) return st;
   if (int st = ensure_smem(kb, geom.smb)) return st;
   for (int e = 0; e < kNumEpilogues; ++e)
@@ -381,11 +345,7 @@ int launch_a(const ff_vort* h, const void* probs, const void* work, int nwork, i
 
 template <typename T>
 int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, cudaStream_t s) {
-  PassLaunch L{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg};
-  L.stage_off = h->g.b_stage_off;
-  L.stage_sz = h->g.b_stage_sz;
-  L.lean = h->g.b_lean;
-  return vort_launch_b<T>(L, probs, work, nwork, s);
+  return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg}, probs, work, nwork, s);
 }
 
 template <typename T, int EPI>
@@ -601,9 +561,7 @@ int ff_vort_config(const ff_vort* h, int32_t cfg[8]) {
   cfg[0] = h->g.tla;
   cfg[1] = h->g.tlc;
   cfg[2] = h->g.tlr;
-  // -1: register-resident power-of-two path; -2: the same with pass B staged through shared
-  // memory; -3: the same with the lean pass B
-  cfg[3] = h->g.reg ? (h->g.b_lean ? -3 : (h->g.b_stage_sz > 0 ? -2 : -1)) : h->g.radix_variant;
+  cfg[3] = h->g.reg ? -1 : h->g.radix_variant;  // -1: register-resident power-of-two path
   cfg[4] = h->g.tha;
   cfg[5] = h->g.thb;
   cfg[6] = h->g.thc;
@@ -625,9 +583,8 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   const int reps = steps_per_trial > 0 ? steps_per_trial : 3;
   const int tls_f64[] = {1, 2, 4, 8};
   const int tls_f32[] = {1, 2, 4, 8};
-  // the generic path varies the radix order; the register path has one stage schedule and
-  // varies pass B (direct loads, inputs staged through shared memory, the lean form)
-  const int nvar = 3;
+  // the register path has one stage schedule; only the generic path varies radix order
+  const int nvar = reg_capable(h) ? 1 : 3;
   const int* tls = h->prec == FF_F64 ? tls_f64 : tls_f32;
   const int ntl = 4;
   double best = 1e30;

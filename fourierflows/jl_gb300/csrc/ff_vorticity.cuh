@@ -541,11 +541,8 @@ __device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __
 
 // Loads go straight from W (an L2 prefetch one item ahead, see k_vort_b_r) into
 // registers; shared memory holds only the exchanges.
-// STAGED: the rows come from `stage`, the shared-memory copy of this item's rows (field f,
-// row ln at (f * rows + ln) * nkp); otherwise straight from W
-template <typename T, int H, bool STAGED>
-__device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>* smem,
-                                           const cx<T>* __restrict__ stage) {
+template <typename T, int H>
+__device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>* smem) {
   constexpr int PP = H / 8;
   constexpr int SH = sizeof(T) == 8 ? 3 : 4;
   constexpr int STRIDE = H + (H >> SH) + 1;
@@ -554,12 +551,10 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   const int j = tile * rows + ln;
   const int ny = P.ny, nkd = P.nkd, nkp = P.nkp;
   const int fstride = nkp * ny;
-  const cx<T>* xbase = STAGED ? stage + ln * nkp : P.W + j * nkp;
-  const int xfs = STAGED ? rows * nkp : fstride;
   cx<T> v[3][8];
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
-    const cx<T>* src = xbase + f * xfs;
+    const cx<T>* src = P.W + f * fstride + j * nkp;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = t + q * PP;
@@ -619,72 +614,6 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
     }
   }
   __syncthreads();
-}
-
-// Pass B with one transformed field in registers besides zeta: C2R of zeta, then for u and
-// v in turn C2R, the product with zeta and R2C.  Each field goes through the same
-// operations as in vort_b_reg (bit-identical results) with a third of the registers held
-// across the transforms, so more rows are in flight per SM (FP32).
-template <typename T, int H>
-__device__ __forceinline__ void vort_b_reg_lean(const VortProb<T>& P, int tile, cx<T>* smem) {
-  constexpr int PP = H / 8;
-  constexpr int SH = sizeof(T) == 8 ? 3 : 4;
-  constexpr int STRIDE = H + (H >> SH) + 1;
-  const int rows = blockDim.x / PP;
-  const int ln = threadIdx.x / PP, t = threadIdx.x & (PP - 1);
-  const int j = tile * rows + ln;
-  const int ny = P.ny, nkd = P.nkd, nkp = P.nkp;
-  const int fstride = nkp * ny;
-  const XRow xr{ln * STRIDE, SH};
-  cx<T>* const buf[1] = {smem};
-  auto load = [&](int f, cx<T>(&v)[1][8]) {
-    const cx<T>* src = P.W + f * fstride + j * nkp;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int k = t + q * PP;
-      cx<T> val = czero<T>();
-      if (j < ny) {
-        const cx<T> xk = k < nkd ? src[k] : czero<T>();
-        const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
-        val = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]), k);
-      }
-      v[0][q] = val;
-    }
-  };
-  cx<T> z[1][8];
-  load(2, z);
-  regfft<T, 1, H, 1>(z, t, P.twx, buf, xr);
-  const T s2 = P.scale2;
-#pragma unroll 1
-  for (int f = 0; f < 2; ++f) {
-    cx<T> v[1][8];
-    load(f, v);
-    regfft<T, 1, H, 1>(v, t, P.twx, buf, xr);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) v[0][q] = mk<T>(v[0][q].x * z[0][q].x * s2, v[0][q].y * z[0][q].y * s2);
-    regfft<T, 1, H, -1>(v, t, P.twx, buf, xr);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) smem[xr(t + q * PP)] = v[0][q];
-    __syncthreads();
-    if (j < ny) {
-      cx<T>* qf = P.Q + f * fstride + j * nkp;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int k = t + q * PP;
-        if (k >= nkd) continue;
-        cx<T> x, dummy;
-        if (k == 0) {
-          const cx<T> z0 = v[0][0];
-          x = mk<T>(z0.x + z0.y, T(0));
-          if (nkd > H) qf[H] = mk<T>(z0.x - z0.y, T(0));  // no dealiasing: the Nyquist column too
-        } else {
-          r2c_pair<T>(v[0][q], smem[xr(H - k)], __ldg(&P.rtw[k]), x, dummy);
-        }
-        qf[k] = x;
-      }
-    }
-    __syncthreads();
-  }
 }
 
 // epilogue of thread t's eight elements (rows t + q NY/8) of column c: the loads of a
@@ -895,88 +824,13 @@ template <typename T> __device__ __forceinline__ void prefetch_b(const VortProb<
     prefetch_lines(P.W + f * fstride + j0 * P.nkp, nr * P.nkp, threadIdx.x, blockDim.x);
 }
 
-// 16-byte asynchronous copies global -> shared (no registers held, no completion to poll:
-// cp.async.wait_group returns when this thread's older groups have landed)
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
-// every 16-byte chunk of item it's three W row blocks into `stage` (field f, row r at
-// (f * rows + r) * nkp; nkp complex values are a whole number of chunks)
-template <typename T> __device__ __forceinline__ void stage_b(const VortProb<T>& P, const WorkItem& it, cx<T>* stage) {
-  const int rows = blockDim.x * 8 / (P.nx / 2), j0 = it.tile * rows;
-  const int nr = min(rows, P.ny - j0);
-  if (nr <= 0) return;
-  constexpr int E = 16 / (int)sizeof(cx<T>);  // complex values per chunk
-  const int nkp = P.nkp, cpr = nkp / E;
-  const int64_t fstride = (int64_t)nkp * P.ny;
-  const int total = 3 * nr * cpr;
-  for (int c = threadIdx.x; c < total; c += blockDim.x) {
-    const int fr = c / cpr, k = (c - fr * cpr) * E;
-    const int f = fr / nr, r = fr - f * nr;
-    cp_async16(stage + (f * rows + r) * nkp + k, P.W + f * fstride + (int64_t)(j0 + r) * nkp + k);
-  }
-}
-
-// Pass B, persistent over row blocks.  STAGED: each item's W rows are copied into one of
-// two shared-memory stages (at byte offsets stage_off and stage_off + stage_sz) while the
-// previous item is transformed, so the transforms read their inputs from shared memory.
-// Otherwise direct loads, with the next item's rows prefetched into L2.
-template <typename T, bool STAGED>
-__global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restrict__ probs,
-                                                  const WorkItem* __restrict__ work, int nwork, int stage_off,
-                                                  int stage_sz) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
-  cx<T>* const stage0 = reinterpret_cast<cx<T>*>(smem_raw + stage_off);
-  cx<T>* const stage1 = reinterpret_cast<cx<T>*>(smem_raw + stage_off + stage_sz);
-  if (STAGED) {
-    if ((int)blockIdx.x < nwork) {
-      const WorkItem it0 = work[blockIdx.x];
-      stage_b(probs[it0.prob], it0, stage0);
-    }
-    cp_async_commit();
-  }
-  int i = 0;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x, ++i) {
-    const WorkItem it = work[w];
-    const VortProb<T>& P = probs[it.prob];
-    const int wn = w + (int)gridDim.x;
-    if (STAGED) {
-      // the stage written here was last read by the item before, which ended with a barrier
-      if (wn < nwork) {
-        const WorkItem nxt = work[wn];
-        stage_b(probs[nxt.prob], nxt, (i & 1) ? stage0 : stage1);
-      }
-      cp_async_commit();
-      cp_async_wait<1>();  // this item's copies (every group but the newest) have landed
-      __syncthreads();
-    } else if (wn < nwork) {
-      const WorkItem nxt = work[wn];
-      prefetch_b(probs[nxt.prob], nxt);
-    }
-    const cx<T>* st = (i & 1) ? stage1 : stage0;
-    switch (P.nx / 2) {
-#define FF_B_CASE(N) \
-  case N: vort_b_reg<T, N, STAGED>(P, it.tile, smem, st); break;
-      FF_REG_CASES_B(FF_B_CASE)
-#undef FF_B_CASE
-      default: break;
-    }
-  }
-  if (STAGED) cp_async_wait<0>();
-}
-
-// Pass B, lean form (vort_b_reg_lean): three CTAs of FF_LB_B_THREADS per SM bound the
-// registers (85 per thread), so 64-thread CTAs hold up to 24 warps per SM
+// Pass B, persistent over row blocks; each item's rows are prefetched into L2 one item
+// ahead.  (Staging the rows through shared memory with cp.async one item ahead measured
+// 23% slower, a bulk-copy pipeline 5%, and a form holding one field besides zeta in
+// registers at a time 10%, at 32 x 1024^2 FP32.)
 template <typename T>
-__global__ void __launch_bounds__(FF_LB_B_THREADS, 3) k_vort_b_r_lean(const VortProb<T>* __restrict__ probs,
-                                                                    const WorkItem* __restrict__ work, int nwork) {
+__global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restrict__ probs,
+                                                  const WorkItem* __restrict__ work, int nwork) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -988,7 +842,7 @@ __global__ void __launch_bounds__(FF_LB_B_THREADS, 3) k_vort_b_r_lean(const Vort
     }
     switch (P.nx / 2) {
 #define FF_B_CASE(N) \
-  case N: vort_b_reg_lean<T, N>(P, it.tile, smem); break;
+  case N: vort_b_reg<T, N>(P, it.tile, smem); break;
       FF_REG_CASES_B(FF_B_CASE)
 #undef FF_B_CASE
       default: break;

@@ -300,12 +300,8 @@ typedef struct {
 int ff_vort_adj_nu_terms(ff_vadj* h, const ff_adj_nu* args, double scale, double* dev_acc, void* stream);
 
 /* Launch geometry: cfg = {tile A, tile C, rows B, radix order, threads A, B, C, graph};
- * radix order -1 marks the register-resident power-of-two path, -2 the same with pass B
- * staging its input rows through shared memory, -3 the same with the lean pass B (one
- * field besides zeta in registers at a time).  set_config's radix_variant (0..2) picks the
- * generic path's radix order; on the register path in FP32 variant 1 stages pass B's input
- * rows through shared memory and variant 2 selects the lean pass B (default 0: direct
- * loads, all three fields); FP64 pass B always takes the default. */
+ * radix order -1 marks the register-resident power-of-two path.  set_config's
+ * radix_variant (0..2) picks the generic path's radix order. */
 int ff_vort_config(const ff_vort* h, int32_t cfg[8]);
 int ff_vort_set_config(ff_vort* h, int tla, int tlc, int tlr, int radix_variant);
 
