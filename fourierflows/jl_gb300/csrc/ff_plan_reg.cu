@@ -65,14 +65,37 @@ __device__ __forceinline__ void c2r_row(const cx<T>* __restrict__ in, T* __restr
   const int64_t row = (int64_t)blockIdx.x * rows + ln;
   const bool live = row < nrows;
   const cx<T>* r = in + (live ? row : 0) * (int64_t)(H + 1);
+  const XRow xr{ln * STRIDE, SH};
+  // packing by pairs: k = t + q PP (q < 4) gives Z[k] = A + i P and Z[H-k] = conj(A) + i conj(P)
+  // from A = X[k] + conj X[H-k] and P = (X[k] - conj X[H-k]) conj(W^k); the partner value
+  // reaches its owner through shared memory, Z[0] and the self-paired Z[H/2] directly
   cx<T> v[1][8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
+  for (int q = 0; q < 4; ++q) {
     const int k = t + q * PP;
-    v[0][q] = live ? c2r_pre<T>(r[k], r[H - k], __ldg(&rtw[k]), k) : czero<T>();
+    cx<T> zk = czero<T>(), zh = czero<T>();
+    if (live) {
+      if (k == 0) {
+        zk = c2r_pre<T>(r[0], r[H], __ldg(&rtw[0]), 0);
+      } else {
+        const cx<T> b = conj(r[H - k]);
+        const cx<T> xk = r[k];
+        const cx<T> a = add(xk, b);
+        const cx<T> pp = cmulc(sub(xk, b), __ldg(&rtw[k]));
+        zk = add(a, mul_i(pp));
+        zh = mk<T>(a.x + pp.y, pp.x - a.y);
+      }
+    }
+    v[0][q] = zk;
+    if (k != 0) smem[xr(H - k)] = zh;
   }
+  if (t == 0) smem[xr(H / 2)] = live ? c2r_pre<T>(r[H / 2], r[H / 2], __ldg(&rtw[H / 2]), H / 2) : czero<T>();
+  __syncthreads();
+#pragma unroll
+  for (int q = 4; q < 8; ++q) v[0][q] = smem[xr(t + q * PP)];
+  __syncthreads();
   cx<T>* const buf[1] = {smem};
-  regfft<T, 1, H, 1>(v, t, tw, buf, XRow{ln * STRIDE, SH});
+  regfft<T, 1, H, 1>(v, t, tw, buf, xr);
   if (live) {
     cx<T>* o = reinterpret_cast<cx<T>*>(out + row * (2 * (int64_t)H));
 #pragma unroll

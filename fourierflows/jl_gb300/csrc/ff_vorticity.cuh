@@ -551,25 +551,49 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   const int j = tile * rows + ln;
   const int ny = P.ny, nkd = P.nkd, nkp = P.nkp;
   const int fstride = nkp * ny;
+  const int bufsz = rows * STRIDE;
+  cx<T>* const buf3[3] = {smem, smem + bufsz, smem + 2 * bufsz};
+  const XRow xr{ln * STRIDE, SH};
+  // C2R packing by pairs: for k = t + q PP, q < 4, A = X[k] + conj X[H-k] and
+  // P = (X[k] - conj X[H-k]) conj(W^k) give both Z[k] = A + i P (this thread's slot q) and
+  // Z[H-k] = conj(A) + i conj(P) (slot 7-q of thread PP-t), since X[H-k] + conj X[k] =
+  // conj(A) and W^(H-k) = -conj(W^k).  Partner values go through shared memory; Z[0] and
+  // the self-paired Z[H/2] are formed directly.
   cx<T> v[3][8];
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
     const cx<T>* src = P.W + f * fstride + j * nkp;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < 4; ++q) {
       const int k = t + q * PP;
-      cx<T> val = czero<T>();
+      cx<T> zk = czero<T>(), zh = czero<T>();
       if (j < ny) {
         const cx<T> xk = k < nkd ? src[k] : czero<T>();
         const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
-        val = c2r_pre<T>(xk, xh, __ldg(&P.rtw[k]), k);
+        if (k == 0) {
+          zk = c2r_pre<T>(xk, xh, __ldg(&P.rtw[0]), 0);
+        } else {
+          const cx<T> b = conj(xh);
+          const cx<T> a = add(xk, b);
+          const cx<T> pp = cmulc(sub(xk, b), __ldg(&P.rtw[k]));
+          zk = add(a, mul_i(pp));
+          zh = mk<T>(a.x + pp.y, pp.x - a.y);
+        }
       }
-      v[f][q] = val;
+      v[f][q] = zk;
+      if (k != 0) buf3[f][xr(H - k)] = zh;
+    }
+    if (t == 0) {
+      const cx<T> xm = (j < ny && H / 2 < nkd) ? src[H / 2] : czero<T>();
+      buf3[f][xr(H / 2)] = j < ny ? c2r_pre<T>(xm, xm, __ldg(&P.rtw[H / 2]), H / 2) : czero<T>();
     }
   }
-  const int bufsz = rows * STRIDE;
-  cx<T>* const buf3[3] = {smem, smem + bufsz, smem + 2 * bufsz};
-  const XRow xr{ln * STRIDE, SH};
+  __syncthreads();
+#pragma unroll
+  for (int f = 0; f < 3; ++f)
+#pragma unroll
+    for (int q = 4; q < 8; ++q) v[f][q] = buf3[f][xr(t + q * PP)];
+  __syncthreads();
   regfft<T, 3, H, 1>(v, t, P.twx, buf3, xr);
   // products u zeta and v zeta in physical space (packed real pairs), normalisation folded in
   const T s2 = P.scale2;
