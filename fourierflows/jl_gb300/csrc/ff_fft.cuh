@@ -328,6 +328,13 @@ template <typename T> __device__ __forceinline__ void r2c_pair(cx<T> zk, cx<T> z
   xhk = conj(sub(e, wo));
 }
 
+// X[k] of r2c_pair when Z was computed from the signal scaled by 1/2: E and W O without
+// their halvings.  Halving is exact, so the result is r2c_pair's bit for bit.
+template <typename T> __device__ __forceinline__ cx<T> r2c_first_prescaled(cx<T> zk, cx<T> zhk, cx<T> w) {
+  const cx<T> b = conj(zhk);
+  return add(add(zk, b), cmul(mul_mi(sub(zk, b)), w));
+}
+
 // Inverse: 2 Z[k] = (X[k] + conj X[h-k]) + i conj(W_N^k) (X[k] - conj X[h-k]); the
 // unnormalised length-h inverse of 2Z is N times the packed real signal.  At k = 0 only
 // the real parts of X[0] and X[h] enter, the projection onto real signals that FFTW's

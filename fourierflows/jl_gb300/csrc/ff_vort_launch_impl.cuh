@@ -55,6 +55,7 @@ static void launch_c_epi(const PassLaunch& L, const VortProb<T>* P, const WorkIt
   }
 }
 
+#if FF_C_FAMILY_ETD || FF_C_FAMILY_RK
 // pass C launchers of one family of epilogues (compiled in their own translation units):
 // ETD = the bare calcN! and the ETDRK4 substeps, RK = the RK4 substeps and the LSRK54 stage
 template <typename T>
@@ -100,6 +101,8 @@ template <typename T> const void* vort_kernel_c_family(bool reg, int epi, bool f
     default: return nullptr;
   }
 }
+
+#endif
 
 template <typename T> const void* vort_kernel_a(bool reg) {
   return reg ? (const void*)k_vort_a_r<T> : (const void*)k_vort_a<T>;

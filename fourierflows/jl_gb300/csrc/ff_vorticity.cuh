@@ -595,8 +595,10 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
     for (int q = 4; q < 8; ++q) v[f][q] = buf3[f][xr(t + q * PP)];
   __syncthreads();
   regfft<T, 3, H, 1>(v, t, P.twx, buf3, xr);
-  // products u zeta and v zeta in physical space (packed real pairs), normalisation folded in
-  const T s2 = P.scale2;
+  // products u zeta and v zeta in physical space (packed real pairs), normalisation folded
+  // in, and the unpack's two halvings too (s2 / 2: exact, so the unpacked values are those
+  // of the unhalved form bit for bit)
+  const T s2 = P.scale2 * T(0.5);
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const cx<T> z = v[2][q];
@@ -619,19 +621,19 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
     for (int q = 0; q < 8; ++q) {
       const int k = t + q * PP;
       if (k >= nkd) continue;
-      cx<T> x0, x1, dummy;
-      if (k == 0) {
+      cx<T> x0, x1;
+      if (k == 0) {  // Z is half the packed transform here: double X[0] (and X[H]) back
         const cx<T> z0 = p[0][0], z1 = p[1][0];
-        x0 = mk<T>(z0.x + z0.y, T(0));
-        x1 = mk<T>(z1.x + z1.y, T(0));
+        x0 = mk<T>((z0.x + z0.y) * T(2), T(0));
+        x1 = mk<T>((z1.x + z1.y) * T(2), T(0));
         if (nkd > H) {  // no dealiasing: the Nyquist column too
-          q0[H] = mk<T>(z0.x - z0.y, T(0));
-          q1[H] = mk<T>(z1.x - z1.y, T(0));
+          q0[H] = mk<T>((z0.x - z0.y) * T(2), T(0));
+          q1[H] = mk<T>((z1.x - z1.y) * T(2), T(0));
         }
       } else {
         const cx<T> w = __ldg(&P.rtw[k]);
-        r2c_pair<T>(p[0][q], buf3[0][xr(H - k)], w, x0, dummy);
-        r2c_pair<T>(p[1][q], buf3[1][xr(H - k)], w, x1, dummy);
+        x0 = r2c_first_prescaled<T>(p[0][q], buf3[0][xr(H - k)], w);
+        x1 = r2c_first_prescaled<T>(p[1][q], buf3[1][xr(H - k)], w);
       }
       q0[k] = x0;
       q1[k] = x1;
