@@ -75,6 +75,8 @@ SIGNATURES = {
     "ff_vort_calcN": [vp, i64, vp, vp, vp],
     "ff_vort_config": [vp, C.POINTER(C.c_int32)],
     "ff_vort_set_config": [vp, i32, i32, i32, i32],
+    "ff_vort_set_split": [vp, i32],
+    "ff_vort_get_split": [vp, C.POINTER(C.c_int32)],
     "ff_vort_autotune": [vp, i32, vp, C.POINTER(f64)],
     "ff_vort_profile": [vp, i32, vp, C.POINTER(f64)],
     "ff_etdrk4_coefficients": [i32, i64, vp, f64, i32, f64, vp, vp, vp, vp, vp],

@@ -85,7 +85,7 @@ int upload_table(const std::vector<double>& t, int prec, void** dev) {
 }
 
 int ensure_smem(const void* func, size_t bytes) {
-  if (bytes <= 48 * 1024) return FF_OK;
+  if (bytes <= 32 * 1024) return FF_OK;  // inside the default 48 KB with any static use here
   FF_CHECK_ARG(bytes <= 227 * 1024, "shared memory request of %zu bytes exceeds 227 KB", bytes);
   static std::mutex mu;
   static std::set<std::pair<const void*, int>> done;
@@ -94,7 +94,14 @@ int ensure_smem(const void* func, size_t bytes) {
   std::lock_guard<std::mutex> lk(mu);
   auto key = std::make_pair(func, dev);
   if (done.count(key)) return FF_OK;
-  FF_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  // both limits, the default 48 KB and the opt-in 227 KB, cover static and dynamic
+  // shared memory together
+  cudaFuncAttributes fa;
+  FF_CUDA(cudaFuncGetAttributes(&fa, func));
+  if (bytes + fa.sharedSizeBytes <= 48 * 1024) return FF_OK;
+  const size_t cap = 227 * 1024 - fa.sharedSizeBytes;
+  FF_CHECK_ARG(bytes <= cap, "shared memory request of %zu bytes exceeds the kernel's %zu", bytes, cap);
+  FF_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
   done.insert(key);
   return FF_OK;
 }

@@ -13,6 +13,7 @@ struct PassLaunch {
   int tile;   // generic path: tile width / rows per CTA
   bool reg;   // register-resident power-of-two kernels
   bool fuse = false;  // pass C, register path: also the next substep's pass A
+  bool split = false; // pass C, register path, not fused: kept tiles split by field
 };
 
 struct EpiArgs {  // precision-independent copy of EpiScalars
@@ -31,10 +32,10 @@ int vort_launch_c_etd_f32(const PassLaunch&, int, const void*, const void*, int,
 int vort_launch_c_rk_f32(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&, cudaStream_t);
 int vort_launch_c_etd_f64(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&, cudaStream_t);
 int vort_launch_c_rk_f64(const PassLaunch&, int, const void*, const void*, int, const EpiArgs&, cudaStream_t);
-const void* vort_kernel_c_etd_f32(bool reg, int epi, bool fuse);
-const void* vort_kernel_c_rk_f32(bool reg, int epi, bool fuse);
-const void* vort_kernel_c_etd_f64(bool reg, int epi, bool fuse);
-const void* vort_kernel_c_rk_f64(bool reg, int epi, bool fuse);
+const void* vort_kernel_c_etd_f32(bool reg, int epi, bool fuse, bool split);
+const void* vort_kernel_c_rk_f32(bool reg, int epi, bool fuse, bool split);
+const void* vort_kernel_c_etd_f64(bool reg, int epi, bool fuse, bool split);
+const void* vort_kernel_c_rk_f64(bool reg, int epi, bool fuse, bool split);
 
 template <typename T>
 inline int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const void* work, int nwork,
@@ -50,10 +51,11 @@ inline int vort_launch_c(const PassLaunch& L, int epi, const void* probs, const 
 // kernel entry points (for occupancy queries and shared-memory limits)
 template <typename T> const void* vort_kernel_a(bool reg);
 template <typename T> const void* vort_kernel_b(bool reg);
-template <typename T> inline const void* vort_kernel_c(bool reg, int epi, bool fuse = false) {
+template <typename T> inline const void* vort_kernel_c(bool reg, int epi, bool fuse = false, bool split = false) {
   const bool etd = epi <= 4;
-  if (sizeof(T) == 8) return etd ? vort_kernel_c_etd_f64(reg, epi, fuse) : vort_kernel_c_rk_f64(reg, epi, fuse);
-  return etd ? vort_kernel_c_etd_f32(reg, epi, fuse) : vort_kernel_c_rk_f32(reg, epi, fuse);
+  if (sizeof(T) == 8)
+    return etd ? vort_kernel_c_etd_f64(reg, epi, fuse, split) : vort_kernel_c_rk_f64(reg, epi, fuse, split);
+  return etd ? vort_kernel_c_etd_f32(reg, epi, fuse, split) : vort_kernel_c_rk_f32(reg, epi, fuse, split);
 }
 
 constexpr int kNumEpilogues = 10;

@@ -49,6 +49,12 @@ static void launch_c_epi(const PassLaunch& L, const VortProb<T>* P, const WorkIt
         return;
       }
     }
+    if constexpr (!FuseA<T>::value) {  // the split form exists where pass C runs unfused
+      if (L.split) {
+        k_vort_c_r<T, EPI, false, true><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, S);
+        return;
+      }
+    }
     k_vort_c_r<T, EPI, false><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, S);
   } else {
     k_vort_c<T, EPI><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, L.tile, S);
@@ -80,17 +86,20 @@ int vort_launch_c_family(const PassLaunch& L, int epi, const void* probs, const 
   return FF_OK;
 }
 
-template <typename T, int EPI> static const void* fuse_ptr(bool fuse) {
+template <typename T, int EPI> static const void* fuse_ptr(bool fuse, bool split) {
   if constexpr (EPI != EPI_N && EPI != EPI_ETD4 && EPI != EPI_RK4) {
     if (fuse) return (const void*)k_vort_c_r<T, EPI, true>;
+  }
+  if constexpr (!FuseA<T>::value) {
+    if (split) return (const void*)k_vort_c_r<T, EPI, false, true>;
   }
   return (const void*)k_vort_c_r<T, EPI, false>;
 }
 
-template <typename T> const void* vort_kernel_c_family(bool reg, int epi, bool fuse) {
+template <typename T> const void* vort_kernel_c_family(bool reg, int epi, bool fuse, bool split) {
   switch (epi) {
 #define FF_EPI_PTR(E) \
-  case E: return !reg ? (const void*)k_vort_c<T, E> : fuse_ptr<T, E>(fuse);
+  case E: return !reg ? (const void*)k_vort_c<T, E> : fuse_ptr<T, E>(fuse, split);
 #if FF_C_FAMILY_ETD
     FF_EPI_PTR(EPI_N) FF_EPI_PTR(EPI_ETD1) FF_EPI_PTR(EPI_ETD2) FF_EPI_PTR(EPI_ETD3) FF_EPI_PTR(EPI_ETD4)
 #endif
@@ -122,6 +131,8 @@ template <typename T> const void* vort_kernel_b(bool reg) {
                            const EpiArgs& a, cudaStream_t s) {                                                   \
     return vort_launch_c_family<T>(L, epi, probs, work, nwork, a, s);                                            \
   }                                                                                                              \
-  const void* vort_kernel_c_##NAME(bool reg, int epi, bool fuse) { return vort_kernel_c_family<T>(reg, epi, fuse); }
+  const void* vort_kernel_c_##NAME(bool reg, int epi, bool fuse, bool split) {                                  \
+    return vort_kernel_c_family<T>(reg, epi, fuse, split);                                                       \
+  }
 
 }  // namespace ff

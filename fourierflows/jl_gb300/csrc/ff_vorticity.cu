@@ -23,6 +23,7 @@ struct Geom {
   int ga = 0, gb = 0, gc = 0;      // grid sizes
   int radix_variant = 0;           // generic path: 0 radix-8 first, 1 radix-4 first, 2 small radix first
   bool reg = false;                // register-resident power-of-two kernels
+  bool split_c = false;            // register path, unfused pass C: kept tiles split by field
 };
 
 int pow2_floor(int v) {
@@ -79,6 +80,8 @@ struct ff_vort {
   void* d_calc_input = nullptr;
   int nwork_a = 0, nwork_b = 0, nwork_c = 0;
   int nwork_c_kept = 0;         // pass C: the kept-column tiles, a prefix of the work list
+  int split_mode = -1;          // pass C split by field: -1 automatic, 0 off, 1 on
+  void* d_cnt = nullptr;        // its arrival counters, one per kept column tile
   std::vector<void*> tables;    // twiddle tables
   void* d_W = nullptr;
   void* d_Q = nullptr;
@@ -142,6 +145,13 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
     smb = std::max(smb, 3 * rows * (size_t)(H + (H >> sh) + 1) * es);
   }
   g.smb = smb;
+  // Pass C split by field where it runs unfused: twice the work items for a grid with
+  // few kept column tiles per SM (one 1024^2 problem: 342 tiles of one column on 152 SMs)
+  if (!FuseA<T>::value) {
+    int64_t tiles = 0;
+    for (const auto& q : h->host) tiles += ceil_div(q.nkd, std::max(1, g.thc * 8 / (int)q.ny));
+    g.split_c = h->split_mode == 1 || (h->split_mode == -1 && tiles < 8 * (int64_t)sm_count());
+  }
   return g;
 }
 
@@ -181,7 +191,14 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   std::vector<VortProb<T>> probs(h->nprob);
   std::vector<WorkItem> wa, wb, wc;
   const size_t es = elem<T>();
-  int64_t woff = 0;
+  int64_t woff = 0, coff = 0;
+  if (h->d_cnt) { cudaFree(h->d_cnt); h->d_cnt = nullptr; }
+  if (geom.split_c) {
+    int64_t tiles = 0;
+    for (const auto& q : h->host) tiles += ceil_div(q.nkd, std::max(1, geom.thc * 8 / (int)q.ny));
+    FF_CUDA(cudaMalloc(&h->d_cnt, sizeof(unsigned) * tiles));
+    FF_CUDA(cudaMemset(h->d_cnt, 0, sizeof(unsigned) * tiles));
+  }
   for (int64_t i = 0; i < h->nprob; ++i) {
     const ff_vort_problem& q = h->host[i];
     VortProb<T>& P = probs[i];
@@ -258,7 +275,14 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
     const int tb = (int)ceil_div(P.ny, wb_);
     for (int tt = 0; tt < tb; ++tt) wb.push_back({(int)i, tt, 0, 0});
     const int tc = (int)ceil_div(P.nkr, wc_);
-    for (int tt = 0; tt < tc; ++tt) wc.push_back({(int)i, tt, 0, 0});
+    for (int tt = 0; tt < tc; ++tt) {
+      wc.push_back({(int)i, tt, 0, 0});
+      if (geom.split_c && tt * wc_ < P.nkd) wc.push_back({(int)i, tt, 1, 0});
+    }
+    if (geom.split_c) {
+      P.cnt = (unsigned*)h->d_cnt + coff;
+      coff += ceil_div(P.nkd, wc_);
+    }
   }
   // longest work first helps the persistent grid balance uneven sizes
   auto by_size = [&](const WorkItem& a, const WorkItem& b) {
@@ -325,11 +349,12 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   if (int st = ensure_smem(kb, geom.smb)) return st;
   for (int e = 0; e < kNumEpilogues; ++e)
     for (bool fuse : {false, true})
-      if (int st = ensure_smem(vort_kernel_c<T>(geom.reg, e, fuse), geom.smc)) return st;
+      for (bool split : {false, true})
+        if (int st = ensure_smem(vort_kernel_c<T>(geom.reg, e, fuse, split), geom.smc)) return st;
   h->g.ga = grid_for<T>(ka, geom.tha, geom.sma, h->nwork_a);
   h->g.gb = grid_for<T>(kb, geom.thb, geom.smb, h->nwork_b);
-  h->g.gc = grid_for<T>(vort_kernel_c<T>(geom.reg, EPI_ETD1, geom.reg && FuseA<T>::value), geom.thc, geom.smc,
-                        h->nwork_c);
+  h->g.gc = grid_for<T>(vort_kernel_c<T>(geom.reg, EPI_ETD1, geom.reg && FuseA<T>::value, geom.split_c), geom.thc,
+                        geom.smc, h->nwork_c);
   if (h->exec) { cudaGraphExecDestroy(h->exec); h->exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
   return FF_OK;
@@ -348,12 +373,15 @@ int launch_b(const ff_vort* h, const void* probs, const void* work, int nwork, i
   return vort_launch_b<T>(PassLaunch{grid, h->g.thb, h->g.smb, h->g.tlr, h->g.reg}, probs, work, nwork, s);
 }
 
+// split: the work list holds the kept tiles split by field (the step's own list; the
+// single-problem calcN! list is never split)
 template <typename T, int EPI>
 int launch_c(const ff_vort* h, const void* probs, const void* work, int nwork, int grid, EpiScalars<T> S,
-             cudaStream_t s, bool fuse = false) {
+             cudaStream_t s, bool fuse = false, bool split = false) {
   const EpiArgs a{(double)S.c, (double)S.b, (double)S.dt, S.first, S.use_filter};
   PassLaunch L{grid, h->g.thc, h->g.smc, h->g.tlc, h->g.reg};
   L.fuse = fuse;
+  L.split = split;
   return vort_launch_c<T>(L, EPI, probs, work, nwork, a, s);
 }
 
@@ -384,7 +412,7 @@ int calc(const ff_vort* h, const void* inputs, EpiScalars<T> S, cudaStream_t s, 
   const bool kept_only = h->g.reg && (EPI == EPI_ETD1 || EPI == EPI_ETD2 || EPI == EPI_ETD3 || EPI == EPI_RK1 ||
                                       EPI == EPI_RK2 || EPI == EPI_RK3);
   return launch_c<T, EPI>(h, h->d_probs, h->d_work_c, kept_only ? h->nwork_c_kept : h->nwork_c, h->g.gc, S, s,
-                          fused && !last);
+                          fused && !last, h->g.split_c);
 }
 
 template <typename T> int enqueue_step(const ff_vort* h, cudaStream_t s) {
@@ -465,7 +493,7 @@ void destroy(ff_vort* h) {
   if (h->graph) cudaGraphDestroy(h->graph);
   for (void* p : h->tables) cudaFree(p);
   for (void* p : {h->d_probs, h->d_calc_prob, h->d_work_a, h->d_work_b, h->d_work_c, h->d_calc_work, h->d_inputs,
-                  h->d_calc_input, h->d_W, h->d_Q})
+                  h->d_calc_input, h->d_W, h->d_Q, h->d_cnt})
     if (p) cudaFree(p);
   delete h;
 }
@@ -576,6 +604,20 @@ int ff_vort_set_config(ff_vort* h, int tla, int tlc, int tlr, int radix_variant)
   return rebuild(h, tla, tlc, tlr, radix_variant);
 }
 
+int ff_vort_set_split(ff_vort* h, int mode) {
+  FF_CHECK_ARG(h, "ff_vort_set_split: null handle");
+  FF_CHECK_ARG(mode >= -1 && mode <= 1, "ff_vort_set_split: mode -1 (automatic), 0 or 1");
+  FF_CUDA(cudaDeviceSynchronize());
+  h->split_mode = mode;
+  return rebuild(h, h->g.tla, h->g.tlc, h->g.tlr, h->g.radix_variant);
+}
+
+int ff_vort_get_split(const ff_vort* h, int32_t* on) {
+  FF_CHECK_ARG(h && on, "ff_vort_get_split: null argument");
+  *on = h->g.split_c ? 1 : 0;
+  return FF_OK;
+}
+
 int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best_ms) {
   FF_CHECK_ARG(h, "ff_vort_autotune: null handle");
   // The trial steps advance the state: callers pass a scratch copy or restore it.
@@ -583,21 +625,27 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   const int reps = steps_per_trial > 0 ? steps_per_trial : 3;
   const int tls_f64[] = {1, 2, 4, 8};
   const int tls_f32[] = {1, 2, 4, 8};
-  // the register path has one stage schedule; only the generic path varies radix order
+  // the register path has one stage schedule; only the generic path varies radix order,
+  // and only the register path's unfused pass C can be split by field
   const int nvar = reg_capable(h) ? 1 : 3;
+  const bool fused_c = h->prec == FF_F64 ? FuseA<double>::value : FuseA<float>::value;
+  const int nsplit = reg_capable(h) && !fused_c ? 2 : 1;
   const int* tls = h->prec == FF_F64 ? tls_f64 : tls_f32;
   const int ntl = 4;
   double best = 1e30;
-  int bcfg[4] = {0, 0, 0, 0};
+  int bcfg[5] = {0, 0, 0, 0, -1};
   cudaEvent_t e0, e1;
   FF_CUDA(cudaEventCreate(&e0));
   FF_CUDA(cudaEventCreate(&e1));
   int st = FF_OK;
+  const int user_split = h->split_mode;
+  for (int sp = 0; sp < nsplit && st == FF_OK; ++sp)
   for (int v = 0; v < nvar && st == FF_OK; ++v)
     for (int ia = 0; ia < ntl && st == FF_OK; ++ia)
       for (int ic = 0; ic < ntl && st == FF_OK; ++ic)
         for (int ir = 0; ir < ntl && st == FF_OK; ++ir) {
           FF_CUDA(cudaStreamSynchronize(s));
+          h->split_mode = nsplit > 1 ? sp : user_split;
           st = rebuild(h, tls[ia], tls[ic], tls[ir], v);
           if (st) break;
           // skip configurations the size limits clamped to an already tried one
@@ -616,10 +664,12 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
             bcfg[1] = tls[ic];
             bcfg[2] = tls[ir];
             bcfg[3] = v;
+            bcfg[4] = h->split_mode;
           }
         }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  h->split_mode = st ? user_split : bcfg[4];
   if (st) return st;
   FF_CUDA(cudaStreamSynchronize(s));
   if ((st = rebuild(h, bcfg[0], bcfg[1], bcfg[2], bcfg[3]))) return st;
@@ -660,8 +710,10 @@ template <typename T> int profile_t(ff_vort* h, int reps, cudaStream_t s, double
     {
       const int nw = h->g.reg ? h->nwork_c_kept : h->nwork_c;
       const bool fuse = h->g.reg && FuseA<T>::value;
-      st = h->stepper == FF_STEP_RK4 ? launch_c<T, EPI_RK1>(h, h->d_probs, h->d_work_c, nw, h->g.gc, S, s, fuse)
-                                     : launch_c<T, EPI_ETD1>(h, h->d_probs, h->d_work_c, nw, h->g.gc, S, s, fuse);
+      const bool split = h->g.split_c;
+      st = h->stepper == FF_STEP_RK4
+               ? launch_c<T, EPI_RK1>(h, h->d_probs, h->d_work_c, nw, h->g.gc, S, s, fuse, split)
+               : launch_c<T, EPI_ETD1>(h, h->d_probs, h->d_work_c, nw, h->g.gc, S, s, fuse, split);
     }
     if (st) break;
     FF_CUDA(cudaEventRecord(ev[3], s));

@@ -92,6 +92,7 @@ template <typename T> struct VortProb {
   const T* be;
   const T* ga;
   const T* filter;
+  unsigned* cnt;  // pass C split by field: an arrival counter per kept column tile
 };
 
 struct WorkItem {
@@ -729,6 +730,69 @@ __device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, 
   }
 }
 
+__device__ __forceinline__ float mul_nc(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_nc(double a, double b) { return __dmul_rn(a, b); }
+
+// Pass C split by field: work item (tile, f) transforms field f of the tile's kept
+// columns and forms its part of the flux, -i k_f F_f (k_0 = kr, k_1 = l), each product
+// rounded on its own.  The first of the two items to finish leaves its part in its Q
+// columns; the second (an atomic arrival count per tile tells them apart, and resets it)
+// adds the two parts, which gives the same sum whichever field came second, and runs the
+// epilogue.  Nothing waits: twice as many items as column tiles balance a grid that has
+// only a few kept columns per SM.
+template <typename T, int NY, int EPI>
+__device__ __forceinline__ void vort_c_split(const VortProb<T>& P, const EpiScalars<T>& S, int tile, int f,
+                                             cx<T>* smem) {
+  constexpr int PP = NY / 8;
+  const int tl = blockDim.x / PP;
+  const int ln = threadIdx.x & (tl - 1), t = threadIdx.x / tl;
+  const int c = tile * tl + ln;
+  const int nkd = P.nkd, la = P.la, lb = P.lb;
+  const int fstride = P.nkp * P.ny;
+  __shared__ unsigned s_arrived;
+  cx<T> v[1][8];
+  cx<T>* const mine = P.Q + f * fstride + c;
+  // L2 loads: the columns are rewritten below and read back by the other item
+#pragma unroll
+  for (int q = 0; q < 8; ++q) v[0][q] = c < nkd ? __ldcg(mine + (t + q * PP) * P.nkp) : czero<T>();
+  cx<T>* const buf[1] = {smem};
+  regfft<T, 1, NY, -1>(v, t, P.twy, buf, XCol{tl, ln});
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int j = t + q * PP;
+    cx<T> part = czero<T>();
+    if (c < nkd && (j < la || j >= lb)) {
+      const T k = f == 0 ? P.kr[c] : P.l[j];
+      part = mul_mi(mk<T>(mul_nc(v[0][q].x, k), mul_nc(v[0][q].y, k)));
+    }
+    v[0][q] = part;
+  }
+  if (c < nkd) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int j = t + q * PP;
+      if (j < la || j >= lb) __stcg(mine + j * P.nkp, v[0][q]);
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_arrived = atomicInc(P.cnt + tile, 1u);  // 0 -> 1 for the first, 1 -> 0 for the second
+    __threadfence();
+  }
+  __syncthreads();
+  if (s_arrived == 0) return;
+  const cx<T>* const other = P.Q + (1 - f) * fstride + c;
+  cx<T> N[8], next[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int j = t + q * PP;
+    N[q] = czero<T>();
+    if (c < nkd && (j < la || j >= lb)) N[q] = add(v[0][q], __ldcg(other + j * P.nkp));
+  }
+  if (c < P.nkr) epilogue_col<T, NY, EPI>(P, S, c, t, N, next);
+}
+
 // FUSE: also run the next substep's pass A on the new state of this column tile
 template <typename T, int NY, int EPI, bool FUSE>
 __device__ __forceinline__ void vort_c_reg(const VortProb<T>& P, const EpiScalars<T>& S, int tile, cx<T>* smem) {
@@ -876,7 +940,9 @@ __global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restr
   }
 }
 
-template <typename T, int EPI, bool FUSE>
+// SPLIT: pass C split by field (vort_c_split) on the kept column tiles; the work list
+// then holds two items, fields 0 and 1, per kept tile
+template <typename T, int EPI, bool FUSE, bool SPLIT = false>
 __global__ void __launch_bounds__(FF_LB_C) k_vort_c_r(const VortProb<T>* __restrict__ probs,
                                                   const WorkItem* __restrict__ work, int nwork, EpiScalars<T> S) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -884,9 +950,13 @@ __global__ void __launch_bounds__(FF_LB_C) k_vort_c_r(const VortProb<T>* __restr
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const WorkItem it = work[w];
     const VortProb<T>& P = probs[it.prob];
+    const bool split = SPLIT && it.tile * (int)(blockDim.x * 8 / P.ny) < P.nkd;
     switch (P.ny) {
-#define FF_C_CASE(N) \
-  case N: vort_c_reg<T, N, EPI, FUSE>(P, S, it.tile, smem); break;
+#define FF_C_CASE(N)                                                       \
+  case N:                                                                  \
+    if (split) vort_c_split<T, N, EPI>(P, S, it.tile, it.field, smem);     \
+    else vort_c_reg<T, N, EPI, FUSE>(P, S, it.tile, smem);                 \
+    break;
       FF_REG_CASES(FF_C_CASE)
 #undef FF_C_CASE
       default: break;

@@ -103,10 +103,18 @@ class FusedStepper:
         cfg = (C.c_int32 * 8)()
         _lib.call("ff_vort_config", self._h, cfg)
         keys = ("tile_a", "tile_c", "rows_b", "radix_order", "threads_a", "threads_b", "threads_c", "graph")
-        return dict(zip(keys, list(cfg)))
+        out = dict(zip(keys, list(cfg)))
+        split = C.c_int32()
+        _lib.call("ff_vort_get_split", self._h, C.byref(split))
+        out["split_c"] = split.value
+        return out
 
     def set_config(self, tile_a, tile_c, rows_b, radix_order=0):
         _lib.call("ff_vort_set_config", self._h, tile_a, tile_c, rows_b, radix_order)
+
+    def set_split(self, mode):
+        """Pass C split by field: -1 automatic, 0 off, 1 on (see ff_vort_set_split)."""
+        _lib.call("ff_vort_set_split", self._h, int(mode))
 
     def autotune(self, steps_per_trial=3, stream=None):
         best = C.c_double()

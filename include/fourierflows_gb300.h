@@ -305,8 +305,18 @@ int ff_vort_adj_nu_terms(ff_vadj* h, const ff_adj_nu* args, double scale, double
 int ff_vort_config(const ff_vort* h, int32_t cfg[8]);
 int ff_vort_set_config(ff_vort* h, int tla, int tlc, int tlr, int radix_variant);
 
-/* Time every tile / radix-order candidate for `steps_per_trial` steps and keep the
- * fastest; the trial steps advance the state, so pass scratch states or restore them. */
+/* Pass C split by field (register path, where pass C does not also run the next pass A):
+ * two work items per kept column tile, one per transformed field, the second to finish
+ * running the epilogue; for grids with few kept column tiles per SM.  mode -1 lets the
+ * library decide from the tile count (the default), 0 and 1 turn it off and on;
+ * get_split reports whether the current geometry uses it.  The sums it forms round each
+ * field's part separately, so its results may differ from the unsplit form's in the last
+ * bit. */
+int ff_vort_set_split(ff_vort* h, int mode);
+int ff_vort_get_split(const ff_vort* h, int32_t* on);
+
+/* Time every tile / radix-order (and split) candidate for `steps_per_trial` steps and keep
+ * the fastest; the trial steps advance the state, so pass scratch states or restore them. */
 int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best_ms);
 
 #ifdef __cplusplus

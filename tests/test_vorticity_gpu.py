@@ -229,6 +229,59 @@ def test_autotune_keeps_results(ff, cuda):
         assert rel(ff.to_numpy(prob.sol), oprob.sol) < 1e-12, cfg
 
 
+@pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredETDRK4", "RK4", "LSRK54", "FilteredLSRK54"])
+def test_split_pass_c_matches_unsplit(ff, cuda, stepper):
+    """FP64 pass C split by field (two work items per kept column tile; the second to
+    finish adds the two flux parts and runs the epilogue) against the unsplit form and the
+    oracle, at one, two and four columns per tile (the last kept tile then also holds
+    aliased columns).  The two forms round the flux sum differently, so they agree to
+    rounding, not bit for bit.  Twenty graph replays from the same state give the same
+    result each time: the arrival counters are reset by every launch."""
+    prob, oprob = make_pair(ff, 128, stepper, ny=64)  # power-of-two lengths: the register path
+    fs = prob.timestepper._native(prob.eqn).ensure(prob.sol, prob.clock)
+    start = prob.sol.clone()
+    orc.stepforward(oprob, 20)
+    outs = {}
+    for split in (0, 1):
+        fs.set_split(split)
+        for tiles in ((1, 1, 1), (2, 2, 2), (4, 4, 1)):
+            fs.set_config(*tiles, 0)
+            assert fs.config()["split_c"] == split
+            prob.sol.copy_(start)
+            fs.advance(20)
+            got = ff.to_numpy(prob.sol)
+            assert rel(got, oprob.sol) < 1e-12, (split, tiles)
+            outs[(split, tiles)] = got
+        prob.sol.copy_(start)
+        fs.advance(20)
+        assert np.array_equal(ff.to_numpy(prob.sol), outs[(split, (4, 4, 1))])
+    assert rel(outs[(1, (1, 1, 1))], outs[(0, (1, 1, 1))]) < 1e-14
+    # automatic choice: one small problem has few kept column tiles, so pass C is split
+    fs.set_split(-1)
+    assert fs.config()["split_c"] == 1
+
+
+def test_split_pass_c_ensemble_and_fp32(ff, cuda):
+    """The split pass C over an uneven FP64 ensemble (arrival counters per problem and
+    tile) matches every member's oracle run; FP32, whose pass C runs the next pass A, never
+    splits."""
+    spec = [(32, 1e-3, 5), (128, 3e-4, 6), (64, 1e-4, 7), (256, 2e-4, 9)]
+    ens = ff.Vorticity.Ensemble(spec, mu=1e-2, dt=2e-3, T=np.float64)
+    ens.fs.set_split(1)
+    assert ens.fs.config()["split_c"] == 1
+    ens.stepforward_(8)
+    for (n, nu, seed), m in zip(spec, ens.members):
+        z0 = ff.Vorticity.random_phase_vorticity(n, seed=seed)
+        op = orc.VorticityProblem(n, 2 * math.pi, nu, 1e-2, 2e-3, "ETDRK4")
+        op.sol[...] = orc.rfft(z0)
+        orc.stepforward(op, 8)
+        assert rel(ff.to_numpy(m.sol), op.sol) < 1e-12, (n, nu)
+    prob, _ = make_pair(ff, 64, "ETDRK4", T=np.float32)
+    fs = prob.timestepper._native(prob.eqn).ensure(prob.sol, prob.clock)
+    fs.set_split(1)
+    assert fs.config()["split_c"] == 0
+
+
 def test_long_horizon_energy_enstrophy_series_fp64(ff, cuda):
     """Over a long horizon (2000 ETDRK4 steps, t = 4, the plain configuration's ν, μ, dt at
     256²) the FP64 GPU path's energy and enstrophy series match the oracle's, every 100
