@@ -51,7 +51,7 @@ static void launch_c_epi(const PassLaunch& L, const VortProb<T>* P, const WorkIt
     }
     if constexpr (!FuseA<T>::value) {  // the split form exists where pass C runs unfused
       if (L.split) {
-        k_vort_c_r<T, EPI, false, true><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, S);
+        k_vort_c_rs<T, EPI><<<L.grid, L.threads, L.smem, s>>>(P, work, nwork, S);
         return;
       }
     }
@@ -91,7 +91,7 @@ template <typename T, int EPI> static const void* fuse_ptr(bool fuse, bool split
     if (fuse) return (const void*)k_vort_c_r<T, EPI, true>;
   }
   if constexpr (!FuseA<T>::value) {
-    if (split) return (const void*)k_vort_c_r<T, EPI, false, true>;
+    if (split) return (const void*)k_vort_c_rs<T, EPI>;
   }
   return (const void*)k_vort_c_r<T, EPI, false>;
 }

@@ -147,7 +147,7 @@ template <typename T> Geom choose_geom_reg(const ff_vort* h, int tla, int tlc, i
   g.smb = smb;
   // Pass C split by field where it runs unfused: twice the work items for a grid with
   // few kept column tiles per SM (one 1024^2 problem: 342 tiles of one column on 152 SMs)
-  if (!FuseA<T>::value) {
+  if (!FuseA<T>::value && g.thc <= FF_SPLIT_C_THREADS) {
     int64_t tiles = 0;
     for (const auto& q : h->host) tiles += ceil_div(q.nkd, std::max(1, g.thc * 8 / (int)q.ny));
     g.split_c = h->split_mode == 1 || (h->split_mode == -1 && tiles < 8 * (int64_t)sm_count());

@@ -876,6 +876,15 @@ template <> struct RegBudget<double> {
 #endif
 #define FF_LB_B FF_LB_B_THREADS, RegBudget<T>::B
 #define FF_LB_C 512, ((EPI == EPI_ETD4 || EPI == EPI_RK4) ? RegBudget<T>::C4 : RegBudget<T>::C)
+// the split pass C: CTAs of at most FF_SPLIT_C_THREADS threads (one 1024-row column or
+// less), FF_SPLIT_C_MIN of them resident per SM
+#ifndef FF_SPLIT_C_THREADS
+#define FF_SPLIT_C_THREADS 128
+#endif
+#ifndef FF_SPLIT_C_MIN
+#define FF_SPLIT_C_MIN 4
+#endif
+#define FF_LB_C_SPLIT FF_SPLIT_C_THREADS, FF_SPLIT_C_MIN
 
 #define FF_REG_CASES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 #define FF_REG_CASES_B(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048)
@@ -942,7 +951,7 @@ __global__ void __launch_bounds__(FF_LB_B) k_vort_b_r(const VortProb<T>* __restr
 
 // SPLIT: pass C split by field (vort_c_split) on the kept column tiles; the work list
 // then holds two items, fields 0 and 1, per kept tile
-template <typename T, int EPI, bool FUSE, bool SPLIT = false>
+template <typename T, int EPI, bool FUSE>
 __global__ void __launch_bounds__(FF_LB_C) k_vort_c_r(const VortProb<T>* __restrict__ probs,
                                                   const WorkItem* __restrict__ work, int nwork, EpiScalars<T> S) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -950,12 +959,38 @@ __global__ void __launch_bounds__(FF_LB_C) k_vort_c_r(const VortProb<T>* __restr
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const WorkItem it = work[w];
     const VortProb<T>& P = probs[it.prob];
-    const bool split = SPLIT && it.tile * (int)(blockDim.x * 8 / P.ny) < P.nkd;
+    switch (P.ny) {
+#define FF_C_CASE(N) \
+  case N: vort_c_reg<T, N, EPI, FUSE>(P, S, it.tile, smem); break;
+      FF_REG_CASES(FF_C_CASE)
+#undef FF_C_CASE
+      default: break;
+    }
+    __syncthreads();
+  }
+}
+
+// Pass C split by field (vort_c_split) on the kept column tiles, whose work list holds two
+// items, fields 0 and 1, per kept tile; aliased tiles run the plain epilogue.  Its own
+// kernel, with a smaller CTA bound than the plain pass C so that more CTAs are resident
+// (columns of up to 8 FF_SPLIT_C_THREADS rows).
+template <typename T, int EPI>
+__global__ void __launch_bounds__(FF_LB_C_SPLIT) k_vort_c_rs(const VortProb<T>* __restrict__ probs,
+                                                         const WorkItem* __restrict__ work, int nwork,
+                                                         EpiScalars<T> S) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* smem = reinterpret_cast<cx<T>*>(smem_raw);
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem it = work[w];
+    const VortProb<T>& P = probs[it.prob];
+    const bool split = it.tile * (int)(blockDim.x * 8 / P.ny) < P.nkd;
     switch (P.ny) {
 #define FF_C_CASE(N)                                                       \
   case N:                                                                  \
-    if (split) vort_c_split<T, N, EPI>(P, S, it.tile, it.field, smem);     \
-    else vort_c_reg<T, N, EPI, FUSE>(P, S, it.tile, smem);                 \
+    if constexpr (N / 8 <= FF_SPLIT_C_THREADS) {                           \
+      if (split) vort_c_split<T, N, EPI>(P, S, it.tile, it.field, smem);   \
+      else vort_c_reg<T, N, EPI, false>(P, S, it.tile, smem);              \
+    }                                                                      \
     break;
       FF_REG_CASES(FF_C_CASE)
 #undef FF_C_CASE
