@@ -12,6 +12,7 @@ LIBNAME = "libfourierflows_gb300.so"
 LIBPATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), LIBNAME)
 
 FF_OK, FF_ERR_ARG, FF_ERR_CUDA, FF_ERR_UNSUPPORTED, FF_ERR_ALLOC, FF_ERR_TIMEOUT = range(6)
+FF_VORT_CALC_SLOTS = 16  # include/fourierflows_gb300.h
 FF_F64, FF_F32 = 0, 1
 FF_COEF_NONE, FF_COEF_REAL, FF_COEF_COMPLEX, FF_COEF_SCALAR = range(4)
 
@@ -76,6 +77,8 @@ SIGNATURES = {
     "ff_vort_config": [vp, C.POINTER(C.c_int32)],
     "ff_vort_set_config": [vp, i32, i32, i32, i32],
     "ff_vort_set_split": [vp, i32],
+    "ff_vort_calcN_bind": [vp, i32, i64, vp, vp],
+    "ff_vort_calcN_slot": [vp, i32, vp],
     "ff_vort_get_split": [vp, C.POINTER(C.c_int32)],
     "ff_vort_autotune": [vp, i32, vp, C.POINTER(f64)],
     "ff_vort_profile": [vp, i32, vp, C.POINTER(f64)],

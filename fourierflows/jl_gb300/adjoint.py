@@ -68,7 +68,7 @@ def etd_coefficient_derivatives(dt, L, dLdnu, ncirc=32, rcirc=1):
 class VorticityAdjoint:
     """Adjoint machinery for one vorticity ETDRK4 problem (``vorticity.Problem``)."""
 
-    def __init__(self, prob, checkpoint_every=50):
+    def __init__(self, prob, checkpoint_every=50, graph=True):
         ts = prob.timestepper
         if not isinstance(ts, ETDRK4TimeStepper) or ts._filtered:
             raise NotImplementedError("the adjoint is implemented for the (unfiltered) ETDRK4 stepper")
@@ -105,13 +105,18 @@ class VorticityAdjoint:
         self.W1 = up((2 * (self.c1 + self.c2) * w).astype(self.T))
         self.W2 = up((-2 * self.c1 * w).astype(self.T))
         self.Nw = up((nxy / w).astype(self.T))
-        names = ("a", "b", "c", "N1", "N2", "N3", "N4", "lam", "lam2", "lam_a", "lam_b", "lam_c", "lN1", "lN2", "lN3",
-                 "lN4", "tmp")
+        names = ("s", "a", "b", "c", "N1", "N2", "N3", "N4", "lam", "lam2", "lam_a", "lam_b", "lam_c", "lN1", "lN2",
+                 "lN3", "lN4", "tmp")
         self.buf = {k: zeros(dev, Ct, self.shape) for k in names}
         import torch
         self.nu_acc = torch.zeros(1, dtype=torch.float64, device="cuda")
         self.checkpoints = {}
         self.nu = nu
+        # the reverse step as two captured CUDA graphs (lam -> lam2 and lam2 -> lam), built
+        # at the first pullback; the four calcN! of a step run from bound slots
+        self.use_graph = bool(graph)
+        self._graphs = None
+        self._slots = None
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -128,31 +133,35 @@ class VorticityAdjoint:
         _lib.call("ff_etdrk4_substep12", self.prec, self.n, ptr(out), _coef(c1, self.n), ptr(x), _coef(c2, self.n),
                   ptr(y), stream_handle())
 
-    def _N(self, out, x):
+    def _N(self, out, x, slot=None):
         p = self.prob
-        V.calcN_(out, x, 0.0, p.clock, p.vars, p.params, p.grid)
+        if slot is None:
+            V.calcN_(out, x, 0.0, p.clock, p.vars, p.params, p.grid)
+        else:
+            V.calcN_._handle(p.grid, p.sol).calcN_slot(self._slots[slot])
 
     def _JT(self, out, s, lam):
         _lib.call("ff_vadj_apply", self._h, ptr(s), ptr(lam), ptr(out), stream_handle())
 
-    def intermediates(self, s):
-        """a, b, c and N1..N4 of the ETDRK4 step from state s (the forward substeps)."""
+    def intermediates(self, s, bound=False):
+        """a, b, c and N1..N4 of the ETDRK4 step from state s (the forward substeps); bound:
+        s is buf["s"] and the calcN! run from the slots bound to these buffers."""
         B, ts, p = self.buf, self.ts, self.prec
         E2, Z = ts.exp_half_Ldt, ts.zeta
-        self._N(B["N1"], s)
+        self._N(B["N1"], s, 0 if bound else None)
         self._axpby(B["a"], E2, s, Z, B["N1"])
-        self._N(B["N2"], B["a"])
+        self._N(B["N2"], B["a"], 1 if bound else None)
         self._axpby(B["b"], E2, s, Z, B["N2"])
-        self._N(B["N3"], B["b"])
+        self._N(B["N3"], B["b"], 2 if bound else None)
         _lib.call("ff_etdrk4_substep3", p, self.n, ptr(B["c"]), _coef(E2, self.n), ptr(B["a"]), _coef(Z, self.n),
                   ptr(B["N1"]), ptr(B["N3"]), stream_handle())
-        self._N(B["N4"], B["c"])
+        self._N(B["N4"], B["c"], 3 if bound else None)
 
-    def adjoint_step(self, s, lam_in, lam_out):
+    def adjoint_step(self, s, lam_in, lam_out, bound=False):
         """lam_out = (d step / d s)^T lam_in at state s; adds the step's viscosity terms."""
         B, ts = self.buf, self.ts
         E, E2, Z, al, be, ga = ts.expLdt, ts.exp_half_Ldt, ts.zeta, ts.alpha, ts.beta, ts.Gamma
-        self.intermediates(s)
+        self.intermediates(s, bound)
         ax = self._axpby
         ax(B["lN4"], ga, lam_in, 0.0, lam_in)
         ax(B["lN1"], al, lam_in, 0.0, lam_in)
@@ -178,6 +187,44 @@ class VorticityAdjoint:
                   stream_handle())
         self._JT(B["tmp"], s, B["lN1"])
         ax(lam_out, 1.0, lam_out, 1.0, B["tmp"])
+
+    def _bind_slots(self):
+        """Four calcN! slots of the grid's calcN! handle, bound to this object's buffers
+        (slots are handed out once per handle and never rebound while a graph uses them);
+        False when the handle has none left."""
+        if self._slots is not None:
+            return True
+        p, B = self.prob, self.buf
+        fs = V.calcN_._handle(p.grid, p.sol)
+        first = getattr(fs, "_next_slot", 0)
+        if first + 4 > _lib.FF_VORT_CALC_SLOTS:
+            return False
+        fs._next_slot = first + 4
+        self._slots = tuple(range(first, first + 4))
+        for slot, (N, x) in zip(self._slots, ((B["N1"], B["s"]), (B["N2"], B["a"]), (B["N3"], B["b"]),
+                                              (B["N4"], B["c"]))):
+            fs.calcN_bind(slot, N, x)
+        self._slot_handle = fs  # the slots' device buffers live as long as the handle
+        return True
+
+    def _capture(self):
+        """The reverse step as two CUDA graphs over fixed buffers: s = buf["s"], and lam ->
+        lam2 or lam2 -> lam.  Each is run once eagerly first (lazy set-up stays out of the
+        capture).  Leaves the scratch buffers and nu_acc modified."""
+        import torch
+        if not self._bind_slots():
+            return None
+        B = self.buf
+        graphs = {}
+        for lin, lout in (("lam", "lam2"), ("lam2", "lam")):
+            self.adjoint_step(B["s"], B[lin], B[lout], bound=True)
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self.adjoint_step(B["s"], B[lin], B[lout], bound=True)
+            graphs[lin] = g
+        torch.cuda.synchronize()
+        return graphs
 
     # ---- forward with checkpoints, backward sweep ---------------------------------------
     def _fused(self):
@@ -219,6 +266,9 @@ class VorticityAdjoint:
         """Gradient at the initial state and d/dnu, given the gradient at the final state;
         forward() must have run."""
         p, fused, B = self.prob, self._fused(), self.buf
+        if self.use_graph and self._graphs is None:
+            self._graphs = self._capture() or False
+        graphs = self._graphs or None
         self.nu_acc.zero_()
         lam = B["lam"]
         lam.copy_(lam_T)
@@ -235,7 +285,11 @@ class VorticityAdjoint:
                 fused.advance(p.sol, p.clock, 1)
                 states.append(p.sol.clone())
             for s in reversed(states):
-                self.adjoint_step(s, lam, other)
+                if graphs is not None:
+                    B["s"].copy_(s)
+                    graphs["lam" if lam is B["lam"] else "lam2"].replay()
+                else:
+                    self.adjoint_step(s, lam, other)
                 lam, other = other, lam
         p.sol.copy_(self.final)
         import torch

@@ -90,6 +90,14 @@ struct ff_vort {
   cudaGraph_t graph = nullptr;
   bool use_graph = true;
   std::vector<unsigned char> calc_host;  // staging for ff_vort_calcN descriptor + work
+  // ff_vort_calcN_bind slots: a descriptor, work lists and input pointer each, staged once
+  struct CalcSlot {
+    void* d = nullptr;
+    int nwa = 0, nwb = 0, nwc = 0;
+    uint64_t gen = 0;
+  };
+  std::vector<CalcSlot> slots;
+  uint64_t gen = 0;  // geometry generation: a rebuild invalidates the bound slots
   std::vector<unsigned char> host_desc;  // host copy of the device descriptors
   size_t calc_cap = 0;
 };
@@ -357,6 +365,7 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
                         geom.smc, h->nwork_c);
   if (h->exec) { cudaGraphExecDestroy(h->exec); h->exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  ++h->gen;
   return FF_OK;
 }
 
@@ -495,6 +504,8 @@ void destroy(ff_vort* h) {
   for (void* p : {h->d_probs, h->d_calc_prob, h->d_work_a, h->d_work_b, h->d_work_c, h->d_calc_work, h->d_inputs,
                   h->d_calc_input, h->d_W, h->d_Q, h->d_cnt})
     if (p) cudaFree(p);
+  for (auto& sl : h->slots)
+    if (sl.d) cudaFree(sl.d);
   delete h;
 }
 
@@ -734,9 +745,11 @@ extern "C" int ff_vort_profile(ff_vort* h, int reps, void* stream, double ms[3])
   return h->prec == FF_F64 ? profile_t<double>(h, reps, s, ms) : profile_t<float>(h, reps, s, ms);
 }
 
-template <typename T> int calcN_t(ff_vort* h, int64_t prob, const void* sol, void* N, cudaStream_t s) {
-  // a single-problem copy of descriptor `prob` with n1 -> N, its own work lists and the
-  // input pointer, staged through a persistent host buffer and copied on the stream
+// a single-problem copy of descriptor `prob` with n1 -> N, its own work lists and the input
+// pointer, laid out as [descriptor | work A | work B | work C | input] in `out`
+template <typename T>
+void calc_stage(const ff_vort* h, int64_t prob, const void* sol, void* N, std::vector<unsigned char>& out, int& nwa,
+                int& nwb, int& nwc) {
   const size_t psz = sizeof(VortProb<T>);
   VortProb<T> P;
   memcpy(&P, h->host_desc.data() + psz * prob, psz);
@@ -752,14 +765,36 @@ template <typename T> int calcN_t(ff_vort* h, int64_t prob, const void* sol, voi
   for (int t = 0; t < (int)ceil_div(P.ny, wb_); ++t) wb.push_back({0, t, 0, 0});
   for (int t = 0; t < (int)ceil_div(P.nkr, wc_); ++t) wc.push_back({0, t, 0, 0});
   const size_t nw = wa.size() + wb.size() + wc.size();
-  const size_t bytes = psz + nw * sizeof(WorkItem) + sizeof(void*);
-  h->calc_host.resize(bytes);
-  unsigned char* hp = h->calc_host.data();
+  out.resize(psz + nw * sizeof(WorkItem) + sizeof(void*));
+  unsigned char* hp = out.data();
   memcpy(hp, &P, psz);
   memcpy(hp + psz, wa.data(), wa.size() * sizeof(WorkItem));
   memcpy(hp + psz + wa.size() * sizeof(WorkItem), wb.data(), wb.size() * sizeof(WorkItem));
   memcpy(hp + psz + (wa.size() + wb.size()) * sizeof(WorkItem), wc.data(), wc.size() * sizeof(WorkItem));
   memcpy(hp + psz + nw * sizeof(WorkItem), &sol, sizeof(void*));
+  nwa = (int)wa.size();
+  nwb = (int)wb.size();
+  nwc = (int)wc.size();
+}
+
+// the three passes of a staged single-problem calcN! (never split: its own work list)
+template <typename T> int calc_launch(const ff_vort* h, const void* dev, int nwa, int nwb, int nwc, cudaStream_t s) {
+  const size_t psz = sizeof(VortProb<T>);
+  const char* base = (const char*)dev;
+  const void* dwa = base + psz;
+  const void* dwb = base + psz + nwa * sizeof(WorkItem);
+  const void* dwc = base + psz + (nwa + nwb) * sizeof(WorkItem);
+  const void* din = base + psz + (nwa + nwb + nwc) * sizeof(WorkItem);
+  if (int st = launch_a<T>(h, base, dwa, nwa, nwa, din, s)) return st;
+  if (int st = launch_b<T>(h, base, dwb, nwb, nwb, s)) return st;
+  return launch_c<T, EPI_N>(h, base, dwc, nwc, nwc, EpiScalars<T>{}, s);
+}
+
+template <typename T> int calcN_t(ff_vort* h, int64_t prob, const void* sol, void* N, cudaStream_t s) {
+  // staged through a persistent host buffer and copied on the stream
+  int nwa, nwb, nwc;
+  calc_stage<T>(h, prob, sol, N, h->calc_host, nwa, nwb, nwc);
+  const size_t bytes = h->calc_host.size();
   if (bytes > h->calc_cap) {
     // grown at most a few times; the free waits for earlier calls that read it
     if (h->d_calc_prob) cudaFree(h->d_calc_prob);
@@ -769,15 +804,28 @@ template <typename T> int calcN_t(ff_vort* h, int64_t prob, const void* sol, voi
   }
   // stream-ordered: kernels of an earlier call on this stream finish first; the host
   // staging buffer may be reused as soon as the call returns (pageable copy)
-  FF_CUDA(cudaMemcpyAsync(h->d_calc_prob, hp, bytes, cudaMemcpyHostToDevice, s));
-  const char* base = (const char*)h->d_calc_prob;
-  const void* dwa = base + psz;
-  const void* dwb = base + psz + wa.size() * sizeof(WorkItem);
-  const void* dwc = base + psz + (wa.size() + wb.size()) * sizeof(WorkItem);
-  const void* din = base + psz + nw * sizeof(WorkItem);
-  if (int st = launch_a<T>(h, base, dwa, (int)wa.size(), (int)wa.size(), din, s)) return st;
-  if (int st = launch_b<T>(h, base, dwb, (int)wb.size(), (int)wb.size(), s)) return st;
-  return launch_c<T, EPI_N>(h, base, dwc, (int)wc.size(), (int)wc.size(), EpiScalars<T>{}, s);
+  FF_CUDA(cudaMemcpyAsync(h->d_calc_prob, h->calc_host.data(), bytes, cudaMemcpyHostToDevice, s));
+  return calc_launch<T>(h, h->d_calc_prob, nwa, nwb, nwc, s);
+}
+
+template <typename T> int calcN_bind_t(ff_vort* h, int slot, int64_t prob, const void* sol, void* N) {
+  std::vector<unsigned char> hp;
+  ff_vort::CalcSlot sl;
+  calc_stage<T>(h, prob, sol, N, hp, sl.nwa, sl.nwb, sl.nwc);
+  if ((size_t)slot >= h->slots.size()) h->slots.resize(slot + 1);
+  ff_vort::CalcSlot& cur = h->slots[slot];
+  FF_CUDA(cudaDeviceSynchronize());  // a bound slot may be in use by queued launches
+  if (cur.d) cudaFree(cur.d);
+  cur = ff_vort::CalcSlot{};
+  FF_CUDA(cudaMalloc(&sl.d, hp.size()));
+  cudaError_t e = cudaMemcpy(sl.d, hp.data(), hp.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(sl.d);
+    return cuda_status(e, "ff_vort_calcN_bind: staging");
+  }
+  sl.gen = h->gen;
+  cur = sl;
+  return FF_OK;
 }
 
 extern "C" int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream) {
@@ -785,4 +833,24 @@ extern "C" int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N,
   FF_CHECK_ARG(prob >= 0 && prob < h->nprob, "ff_vort_calcN: problem index out of range");
   auto s = (cudaStream_t)stream;
   return h->prec == FF_F64 ? calcN_t<double>(h, prob, sol, N, s) : calcN_t<float>(h, prob, sol, N, s);
+}
+
+extern "C" int ff_vort_calcN_bind(ff_vort* h, int slot, int64_t prob, const void* sol, void* N) {
+  FF_CHECK_ARG(h && sol && N, "ff_vort_calcN_bind: null argument");
+  FF_CHECK_ARG(slot >= 0 && slot < FF_VORT_CALC_SLOTS, "ff_vort_calcN_bind: slot %d outside 0..%d", slot,
+               FF_VORT_CALC_SLOTS - 1);
+  FF_CHECK_ARG(prob >= 0 && prob < h->nprob, "ff_vort_calcN_bind: problem index out of range");
+  return h->prec == FF_F64 ? calcN_bind_t<double>(h, slot, prob, sol, N) : calcN_bind_t<float>(h, slot, prob, sol, N);
+}
+
+extern "C" int ff_vort_calcN_slot(ff_vort* h, int slot, void* stream) {
+  FF_CHECK_ARG(h, "ff_vort_calcN_slot: null handle");
+  FF_CHECK_ARG(slot >= 0 && slot < (int)h->slots.size() && h->slots[slot].d, "ff_vort_calcN_slot: slot %d is not bound",
+               slot);
+  const ff_vort::CalcSlot& sl = h->slots[slot];
+  FF_CHECK_ARG(sl.gen == h->gen, "ff_vort_calcN_slot: slot %d was bound before the launch geometry changed; bind it "
+               "again", slot);
+  auto s = (cudaStream_t)stream;
+  return h->prec == FF_F64 ? calc_launch<double>(h, sl.d, sl.nwa, sl.nwb, sl.nwc, s)
+                           : calc_launch<float>(h, sl.d, sl.nwa, sl.nwb, sl.nwc, s);
 }

@@ -124,6 +124,15 @@ class FusedStepper:
     def calcN(self, N, sol, prob=0, stream=None):
         _lib.call("ff_vort_calcN", self._h, int(prob), ptr(sol, "sol"), ptr(N, "N"), stream_handle(stream))
 
+    def calcN_bind(self, slot, N, sol, prob=0):
+        """Stage calcN!(sol) -> N of problem `prob` in a slot once (see ff_vort_calcN_bind);
+        the caller keeps N and sol alive while the slot is used."""
+        _lib.call("ff_vort_calcN_bind", self._h, int(slot), int(prob), ptr(sol, "sol"), ptr(N, "N"))
+
+    def calcN_slot(self, slot, stream=None):
+        """The bound calcN! of a slot: kernel launches only, safe inside a CUDA graph capture."""
+        _lib.call("ff_vort_calcN_slot", self._h, int(slot), stream_handle(stream))
+
     def profile(self, reps=10, stream=None):
         """Average device ms of passes A, B, C (CUDA events inside the library)."""
         ms = (C.c_double * 3)()

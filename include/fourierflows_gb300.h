@@ -264,6 +264,17 @@ int ff_vort_step(ff_vort* h, int64_t nsteps, void* stream);
  * (as ff_vort_step's are); concurrent calls need separate handles. */
 int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stream);
 
+/* ff_vort_calcN with its descriptor staged once.  bind stores problem `prob`'s descriptor,
+ * work lists and the (sol, N) pointers in slot `slot` (0 .. FF_VORT_CALC_SLOTS-1; it
+ * synchronises the device, so not during stream capture); calcN_slot launches the three
+ * passes of a bound slot with no host staging, so it can be captured in a CUDA graph (a
+ * checkpointed adjoint replays one per step).  A later set_config, set_split or autotune
+ * invalidates the slots: calcN_slot then fails until they are bound again.  The same
+ * serialisation rule as ff_vort_calcN applies (the handle's workspace). */
+#define FF_VORT_CALC_SLOTS 16
+int ff_vort_calcN_bind(ff_vort* h, int slot, int64_t prob, const void* sol, void* N);
+int ff_vort_calcN_slot(ff_vort* h, int slot, void* stream);
+
 /* Average device time (ms) of each of the three passes over `reps` launches, timed with
  * CUDA events on `stream`: ms = {A, B, C}; C runs as in the first substep (its epilogue
  * writes only the stepper's intermediate buffers).  ETDRK4 and RK4 handles only

@@ -19,6 +19,22 @@ def test_library_exports_every_header_symbol(ff):
     assert lib.ff_version() == (0 << 16) | (1 << 8)
 
 
+def test_calcN_slot_count_and_argument_errors(ff):
+    """The slot count mirrored in Python is the header's, and the bound-calcN! entry points
+    reject bad arguments before any CUDA call."""
+    import os
+    import re
+    hdr = os.path.join(os.path.dirname(__file__), "..", "include", "fourierflows_gb300.h")
+    m = re.search(r"#define FF_VORT_CALC_SLOTS (\d+)", open(hdr).read())
+    assert m and int(m.group(1)) == ff._lib.FF_VORT_CALC_SLOTS
+    with pytest.raises(ValueError):
+        ff._lib.call("ff_vort_calcN_bind", None, 0, 0, None, None)
+    with pytest.raises(ValueError):
+        ff._lib.call("ff_vort_calcN_slot", None, 0, None)
+    with pytest.raises(ValueError):
+        ff._lib.call("ff_vort_set_split", None, 0)
+
+
 def test_argument_errors_without_a_gpu(ff):
     """Shape/argument validation happens before any CUDA call, so it is testable here."""
     h = C.c_void_p()
