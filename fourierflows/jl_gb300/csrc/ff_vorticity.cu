@@ -634,56 +634,61 @@ int ff_vort_autotune(ff_vort* h, int steps_per_trial, void* stream, double* best
   // The trial steps advance the state: callers pass a scratch copy or restore it.
   auto s = (cudaStream_t)stream;
   const int reps = steps_per_trial > 0 ? steps_per_trial : 3;
-  const int tls_f64[] = {1, 2, 4, 8};
-  const int tls_f32[] = {1, 2, 4, 8};
+  const int tls[] = {1, 2, 4, 8};  // lines per CTA of passes A and C, rows per CTA of B
+  const int ntl = 4;
   // the register path has one stage schedule; only the generic path varies radix order,
   // and only the register path's unfused pass C can be split by field
   const int nvar = reg_capable(h) ? 1 : 3;
   const bool fused_c = h->prec == FF_F64 ? FuseA<double>::value : FuseA<float>::value;
   const int nsplit = reg_capable(h) && !fused_c ? 2 : 1;
-  const int* tls = h->prec == FF_F64 ? tls_f64 : tls_f32;
-  const int ntl = 4;
+  // the events are destroyed and the caller's split mode is kept on every return path
+  struct Guard {
+    ff_vort* h;
+    int split;
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    ~Guard() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+      h->split_mode = split;
+    }
+  } guard{h, h->split_mode};
+  FF_CUDA(cudaEventCreate(&guard.e[0]));
+  FF_CUDA(cudaEventCreate(&guard.e[1]));
   double best = 1e30;
-  int bcfg[5] = {0, 0, 0, 0, -1};
-  cudaEvent_t e0, e1;
-  FF_CUDA(cudaEventCreate(&e0));
-  FF_CUDA(cudaEventCreate(&e1));
-  int st = FF_OK;
-  const int user_split = h->split_mode;
-  for (int sp = 0; sp < nsplit && st == FF_OK; ++sp)
-  for (int v = 0; v < nvar && st == FF_OK; ++v)
-    for (int ia = 0; ia < ntl && st == FF_OK; ++ia)
-      for (int ic = 0; ic < ntl && st == FF_OK; ++ic)
-        for (int ir = 0; ir < ntl && st == FF_OK; ++ir) {
-          FF_CUDA(cudaStreamSynchronize(s));
-          h->split_mode = nsplit > 1 ? sp : user_split;
-          st = rebuild(h, tls[ia], tls[ic], tls[ir], v);
-          if (st) break;
-          // skip configurations the size limits clamped to an already tried one
-          if (h->g.tla != tls[ia] || h->g.tlc != tls[ic] || h->g.tlr != tls[ir]) continue;
-          if ((st = ff_vort_step(h, 1, s))) break;  // warm-up (and graph capture)
-          FF_CUDA(cudaEventRecord(e0, s));
-          if ((st = ff_vort_step(h, reps, s))) break;
-          FF_CUDA(cudaEventRecord(e1, s));
-          FF_CUDA(cudaEventSynchronize(e1));
-          float ms = 0;
-          FF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-          const double per = ms / reps;
-          if (per < best) {
-            best = per;
-            bcfg[0] = tls[ia];
-            bcfg[1] = tls[ic];
-            bcfg[2] = tls[ir];
-            bcfg[3] = v;
-            bcfg[4] = h->split_mode;
+  int bcfg[5] = {0, 0, 0, 0, guard.split};
+  for (int sp = 0; sp < nsplit; ++sp)
+    for (int v = 0; v < nvar; ++v)
+      for (int ia = 0; ia < ntl; ++ia)
+        for (int ic = 0; ic < ntl; ++ic)
+          for (int ir = 0; ir < ntl; ++ir) {
+            FF_CUDA(cudaStreamSynchronize(s));
+            h->split_mode = nsplit > 1 ? sp : guard.split;
+            if (int st = rebuild(h, tls[ia], tls[ic], tls[ir], v)) return st;
+            // skip configurations the size limits clamped to an already tried one, and
+            // split trials whose geometry cannot split
+            if (h->g.tla != tls[ia] || h->g.tlc != tls[ic] || h->g.tlr != tls[ir]) continue;
+            if (nsplit > 1 && sp == 1 && !h->g.split_c) continue;
+            if (int st = ff_vort_step(h, 1, s)) return st;  // warm-up (and graph capture)
+            FF_CUDA(cudaEventRecord(guard.e[0], s));
+            if (int st = ff_vort_step(h, reps, s)) return st;
+            FF_CUDA(cudaEventRecord(guard.e[1], s));
+            FF_CUDA(cudaEventSynchronize(guard.e[1]));
+            float ms = 0;
+            FF_CUDA(cudaEventElapsedTime(&ms, guard.e[0], guard.e[1]));
+            const double per = ms / reps;
+            if (per < best) {
+              best = per;
+              bcfg[0] = tls[ia];
+              bcfg[1] = tls[ic];
+              bcfg[2] = tls[ir];
+              bcfg[3] = v;
+              bcfg[4] = h->split_mode;
+            }
           }
-        }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  h->split_mode = st ? user_split : bcfg[4];
-  if (st) return st;
   FF_CUDA(cudaStreamSynchronize(s));
-  if ((st = rebuild(h, bcfg[0], bcfg[1], bcfg[2], bcfg[3]))) return st;
+  guard.split = bcfg[4];  // the winner's split mode stays
+  h->split_mode = bcfg[4];
+  if (int st = rebuild(h, bcfg[0], bcfg[1], bcfg[2], bcfg[3])) return st;
   if (best_ms) *best_ms = best;
   return FF_OK;
 }
