@@ -282,6 +282,37 @@ def test_split_pass_c_ensemble_and_fp32(ff, cuda):
     assert fs.config()["split_c"] == 0
 
 
+def test_bound_calcN_slots(ff, cuda):
+    """calcN! from a bound slot equals the staged call bit for bit; a geometry change
+    invalidates the slot until it is bound again; bad slots are rejected."""
+    for T in (np.float64, np.float32):
+        prob, oprob = make_pair(ff, 128, "ETDRK4", T=T, ny=64)
+        g = prob.grid
+        fs = ff.Vorticity.calcN_._handle(g, prob.sol)
+        Ct = np.complex128 if T == np.float64 else np.complex64
+        N0 = ff.zeros(ff.GPU(), Ct, (g.nkr, g.ny))
+        N1 = ff.zeros(ff.GPU(), Ct, (g.nkr, g.ny))
+        fs.calcN(N0, prob.sol)
+        fs.calcN_bind(3, N1, prob.sol)
+        fs.calcN_slot(3)
+        assert np.array_equal(ff.to_numpy(N0), ff.to_numpy(N1))
+        No = np.zeros_like(oprob.sol)
+        orc.vorticity_calcN(No, oprob.sol, 0.0, None, None, None, oprob.grid)
+        assert rel(ff.to_numpy(N1).astype(np.complex128), No) < (1e-13 if T == np.float64 else 1e-5)
+        fs.set_config(2, 2, 2, 0)
+        with pytest.raises(ValueError, match="bind it again"):
+            fs.calcN_slot(3)
+        N1.zero_()
+        fs.calcN_bind(3, N1, prob.sol)
+        fs.calcN_slot(3)
+        fs.calcN(N0, prob.sol)
+        assert np.array_equal(ff.to_numpy(N0), ff.to_numpy(N1))
+        with pytest.raises(ValueError):
+            fs.calcN_slot(7)  # never bound
+        with pytest.raises(ValueError):
+            fs.calcN_bind(ff._lib.FF_VORT_CALC_SLOTS, N1, prob.sol)
+
+
 def test_long_horizon_energy_enstrophy_series_fp64(ff, cuda):
     """Over a long horizon (2000 ETDRK4 steps, t = 4, the plain configuration's ν, μ, dt at
     256²) the FP64 GPU path's energy and enstrophy series match the oracle's, every 100
