@@ -67,30 +67,78 @@ template <typename T, int DIR> struct Dft<T, 4, DIR> {
   }
 };
 
+// the radix-8 butterfly after its first layer: a[r] = v[r] + v[r+4], b[r] = v[r] - v[r+4]
+template <typename T, int DIR> __device__ __forceinline__ void dft8_rest(cx<T> (&a)[4], cx<T> (&b)[4], cx<T>* v);
+
 template <typename T, int DIR> struct Dft<T, 8, DIR> {
   static __device__ __forceinline__ void run(cx<T>* v) {
-    const T h = T(FF_SQRT1_2);
     cx<T> a[4], b[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       a[r] = add(v[r], v[r + 4]);
       b[r] = sub(v[r], v[r + 4]);
     }
-    // b[r] *= W8^r (forward W8 = (1 - i)/sqrt2, inverse its conjugate)
-    b[1] = DIR < 0 ? mk<T>(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x))
-                   : mk<T>(h * (b[1].x - b[1].y), h * (b[1].y + b[1].x));
-    b[2] = rot<DIR>(b[2]);
-    b[3] = DIR < 0 ? mk<T>(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y))
-                   : mk<T>(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));
-    Dft<T, 4, DIR>::run(a);
-    Dft<T, 4, DIR>::run(b);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      v[2 * q] = a[q];
-      v[2 * q + 1] = b[q];
-    }
+    dft8_rest<T, DIR>(a, b, v);
   }
 };
+
+// a + u w (DIR < 0) or a + u conj(w) (DIR > 0) as two FMA chains (four FMAs where a product
+// and an add take six operations)
+template <int DIR, typename C> __device__ __forceinline__ C fma_tw(C a, C u, C w) {
+  C r;
+  if (DIR < 0) {
+    r.x = fma(u.x, w.x, fma(-u.y, w.y, a.x));
+    r.y = fma(u.x, w.y, fma(u.y, w.x, a.y));
+  } else {
+    r.x = fma(u.x, w.x, fma(u.y, w.y, a.x));
+    r.y = fma(u.y, w.x, fma(-u.x, w.y, a.y));
+  }
+  return r;
+}
+// 2 t - s (one FMA per part; 2 t is exact)
+template <typename C> __device__ __forceinline__ C twice_minus(C t, C s) {
+  C r;
+  r.x = fma(decltype(t.x)(2), t.x, -s.x);
+  r.y = fma(decltype(t.y)(2), t.y, -s.y);
+  return r;
+}
+
+// Radix-8 butterfly of a twiddled stage, the twiddles w[1..7] applied inside its first
+// layer: with t_r = u_r w_r (t_0 = u_0), a[r] = t_r + u_{r+4} w_{r+4} by FMA chains and
+// b[r] = 2 t_r - a[r], 36 instead of 44 FP64 operations for the twiddles and that layer.
+// Used for FP64, whose kernels are bound by the FP64 pipe; the rounding differs from
+// twiddle-then-butterfly within the FFT's usual error.
+template <typename T, int DIR> struct Dft8Tw {
+  static __device__ __forceinline__ void run(cx<T>* v, const cx<T>* w) {
+    cx<T> a[4], b[4];
+    a[0] = fma_tw<DIR>(v[0], v[4], w[4]);
+    b[0] = twice_minus(v[0], a[0]);
+#pragma unroll
+    for (int r = 1; r < 4; ++r) {
+      const cx<T> t = DIR < 0 ? cmul(v[r], w[r]) : cmulc(v[r], w[r]);
+      a[r] = fma_tw<DIR>(t, v[r + 4], w[r + 4]);
+      b[r] = twice_minus(t, a[r]);
+    }
+    dft8_rest<T, DIR>(a, b, v);
+  }
+};
+
+template <typename T, int DIR> __device__ __forceinline__ void dft8_rest(cx<T> (&a)[4], cx<T> (&b)[4], cx<T>* v) {
+  const T h = T(FF_SQRT1_2);
+  // b[r] *= W8^r (forward W8 = (1 - i)/sqrt2, inverse its conjugate)
+  b[1] = DIR < 0 ? mk<T>(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x))
+                 : mk<T>(h * (b[1].x - b[1].y), h * (b[1].y + b[1].x));
+  b[2] = rot<DIR>(b[2]);
+  b[3] = DIR < 0 ? mk<T>(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y))
+                 : mk<T>(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));
+  Dft<T, 4, DIR>::run(a);
+  Dft<T, 4, DIR>::run(b);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[2 * q] = a[q];
+    v[2 * q + 1] = b[q];
+  }
+}
 
 // FP32 butterflies on Blackwell's packed FP32 instructions.  A float2 complex value is one
 // register pair and FADD2 / FFMA2 / FMUL2 apply one operation to both halves, so an

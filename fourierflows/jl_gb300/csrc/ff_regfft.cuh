@@ -18,6 +18,12 @@
 
 #include "ff_fft.cuh"
 
+// FP64 twiddled radix-8 stages fold their twiddle products into the butterfly's first
+// layer (Dft8Tw); 0 restores twiddle-then-butterfly
+#ifndef FF_TWIDDLE_FMA
+#define FF_TWIDDLE_FMA 1
+#endif
+
 namespace ff {
 
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
@@ -61,11 +67,15 @@ __device__ __forceinline__ void regfft_from(cx<T> (&v)[F][8], int t, const cx<T>
       cx<T> u[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) u[r] = v[f][m + r * M];
-      if (NS > 1) {
+      if constexpr (NS > 1 && R == 8 && FF_TWIDDLE_FMA && sizeof(T) == 8) {
+        Dft8Tw<T, DIR>::run(u, w);  // FP64: the twiddles inside the first butterfly layer
+      } else {
+        if (NS > 1) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) u[r] = DIR < 0 ? cmul(u[r], w[r]) : cmulc(u[r], w[r]);
+          for (int r = 1; r < R; ++r) u[r] = DIR < 0 ? cmul(u[r], w[r]) : cmulc(u[r], w[r]);
+        }
+        Dft<T, R, DIR>::run(u);
       }
-      Dft<T, R, DIR>::run(u);
 #pragma unroll
       for (int r = 0; r < R; ++r) v[f][m + r * M] = u[r];
     }
