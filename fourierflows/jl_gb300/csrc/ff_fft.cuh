@@ -67,6 +67,13 @@ template <typename T, int DIR> struct Dft<T, 4, DIR> {
   }
 };
 
+// FP64 twiddled radix-8 stages fold their twiddle products into the butterfly's first
+// layer (Dft8Tw), and pass B's packing and unpacking fold theirs into FMA chains; 0
+// restores product-then-add everywhere
+#ifndef FF_TWIDDLE_FMA
+#define FF_TWIDDLE_FMA 1
+#endif
+
 // the radix-8 butterfly after its first layer: a[r] = v[r] + v[r+4], b[r] = v[r] - v[r+4]
 template <typename T, int DIR> __device__ __forceinline__ void dft8_rest(cx<T> (&a)[4], cx<T> (&b)[4], cx<T>* v);
 
@@ -125,19 +132,32 @@ template <typename T, int DIR> struct Dft8Tw {
 
 template <typename T, int DIR> __device__ __forceinline__ void dft8_rest(cx<T> (&a)[4], cx<T> (&b)[4], cx<T>* v) {
   const T h = T(FF_SQRT1_2);
-  // b[r] *= W8^r (forward W8 = (1 - i)/sqrt2, inverse its conjugate)
-  b[1] = DIR < 0 ? mk<T>(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x))
-                 : mk<T>(h * (b[1].x - b[1].y), h * (b[1].y + b[1].x));
-  b[2] = rot<DIR>(b[2]);
-  b[3] = DIR < 0 ? mk<T>(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y))
-                 : mk<T>(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));
   Dft<T, 4, DIR>::run(a);
-  Dft<T, 4, DIR>::run(b);
+  if constexpr (sizeof(T) == 8 && FF_TWIDDLE_FMA) {
+    // FP64: b[1] W8 = h r1 and b[3] W8^3 = h r3 with r1, r3 the unscaled rotations; the
+    // factor h then enters the radix-4 butterfly's output FMAs (20 instead of 24 operations)
+    const cx<T> r1 = DIR < 0 ? mk<T>(b[1].x + b[1].y, b[1].y - b[1].x) : mk<T>(b[1].x - b[1].y, b[1].y + b[1].x);
+    const cx<T> r3 = DIR < 0 ? mk<T>(b[3].y - b[3].x, -(b[3].x + b[3].y)) : mk<T>(-(b[3].x + b[3].y), b[3].x - b[3].y);
+    const cx<T> b2 = rot<DIR>(b[2]);
+    const cx<T> s02 = add(b[0], b2), d02 = sub(b[0], b2);
+    const cx<T> r13 = add(r1, r3), e13 = rot<DIR>(sub(r1, r3));
+    v[1] = mk<T>(fma(h, r13.x, s02.x), fma(h, r13.y, s02.y));
+    v[5] = mk<T>(fma(-h, r13.x, s02.x), fma(-h, r13.y, s02.y));
+    v[3] = mk<T>(fma(h, e13.x, d02.x), fma(h, e13.y, d02.y));
+    v[7] = mk<T>(fma(-h, e13.x, d02.x), fma(-h, e13.y, d02.y));
+  } else {
+    // b[r] *= W8^r (forward W8 = (1 - i)/sqrt2, inverse its conjugate)
+    b[1] = DIR < 0 ? mk<T>(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x))
+                   : mk<T>(h * (b[1].x - b[1].y), h * (b[1].y + b[1].x));
+    b[2] = rot<DIR>(b[2]);
+    b[3] = DIR < 0 ? mk<T>(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y))
+                   : mk<T>(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));
+    Dft<T, 4, DIR>::run(b);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    v[2 * q] = a[q];
-    v[2 * q + 1] = b[q];
+    for (int q = 0; q < 4; ++q) v[2 * q + 1] = b[q];
   }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[2 * q] = a[q];
 }
 
 // FP32 butterflies on Blackwell's packed FP32 instructions.  A float2 complex value is one
@@ -287,14 +307,26 @@ __device__ __forceinline__ void fft_stage(const cx<T>* __restrict__ src, cx<T>* 
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[addr(ln, j + r * nb)];
     const int k = j % Ns;
-    if (Ns > 1) {
+    if constexpr (R == 8 && sizeof(T) == 8 && FF_TWIDDLE_FMA) {
+      // FP64: the twiddle products inside the butterfly's first layer (Dft8Tw)
+      if (Ns > 1) {
+        cx<T> w[8];
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        cx<T> w = __ldg(&tw[k * r * tws]);
-        v[r] = DIR < 0 ? cmul(v[r], w) : cmulc(v[r], w);
+        for (int r = 1; r < 8; ++r) w[r] = __ldg(&tw[k * r * tws]);
+        Dft8Tw<T, DIR>::run(v, w);
+      } else {
+        Dft<T, 8, DIR>::run(v);
       }
+    } else {
+      if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          cx<T> w = __ldg(&tw[k * r * tws]);
+          v[r] = DIR < 0 ? cmul(v[r], w) : cmulc(v[r], w);
+        }
+      }
+      Dft<T, R, DIR>::run(v);
     }
-    Dft<T, R, DIR>::run(v);
     const int ob = (j - k) * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[addr(ln, ob + r * Ns)] = v[r];
@@ -381,6 +413,25 @@ template <typename T> __device__ __forceinline__ void r2c_pair(cx<T> zk, cx<T> z
 template <typename T> __device__ __forceinline__ cx<T> r2c_first_prescaled(cx<T> zk, cx<T> zhk, cx<T> w) {
   const cx<T> b = conj(zhk);
   return add(add(zk, b), cmul(mul_mi(sub(zk, b)), w));
+}
+// the same with the twiddle product and its add as two FMA chains (FP64, FP64-pipe bound):
+// 8 instead of 10 operations, rounded differently within the FFT's error
+template <typename T> __device__ __forceinline__ cx<T> r2c_first_prescaled_fma(cx<T> zk, cx<T> zhk, cx<T> w) {
+  const cx<T> b = conj(zhk);
+  const cx<T> e = add(zk, b), m = mul_mi(sub(zk, b));
+  return mk<T>(fma(m.x, w.x, fma(-m.y, w.y, e.x)), fma(m.x, w.y, fma(m.y, w.x, e.y)));
+}
+
+// C2R packing of the pair (k, H-k) from X[k], X[H-k] and W = W_N^k: A = X[k] + conj X[H-k],
+// D = X[k] - conj X[H-k], Z[k] = A + i D conj(W) and Z[H-k] = conj(2A - Z[k]) (= conj(A) +
+// i conj(D conj(W))), the product and its add as two FMA chains: 10 instead of 12 FP64
+// operations
+template <typename T>
+__device__ __forceinline__ void c2r_pair_fma(cx<T> xk, cx<T> xh, cx<T> w, cx<T>& zk, cx<T>& zh) {
+  const cx<T> b = conj(xh);
+  const cx<T> a = add(xk, b), d = sub(xk, b);
+  zk = mk<T>(fma(d.x, w.y, fma(-d.y, w.x, a.x)), fma(d.x, w.x, fma(d.y, w.y, a.y)));
+  zh = mk<T>(fma(T(2), a.x, -zk.x), fma(T(-2), a.y, zk.y));
 }
 
 // Inverse: 2 Z[k] = (X[k] + conj X[h-k]) + i conj(W_N^k) (X[k] - conj X[h-k]); the

@@ -18,12 +18,6 @@
 
 #include "ff_fft.cuh"
 
-// FP64 twiddled radix-8 stages fold their twiddle products into the butterfly's first
-// layer (Dft8Tw); 0 restores twiddle-then-butterfly
-#ifndef FF_TWIDDLE_FMA
-#define FF_TWIDDLE_FMA 1
-#endif
-
 namespace ff {
 
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }

@@ -573,6 +573,8 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
         const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
         if (k == 0) {
           zk = c2r_pre<T>(xk, xh, __ldg(&P.rtw[0]), 0);
+        } else if constexpr (sizeof(T) == 8 && FF_TWIDDLE_FMA) {
+          c2r_pair_fma<T>(xk, xh, __ldg(&P.rtw[k]), zk, zh);
         } else {
           const cx<T> b = conj(xh);
           const cx<T> a = add(xk, b);
@@ -633,8 +635,13 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
         }
       } else {
         const cx<T> w = __ldg(&P.rtw[k]);
-        x0 = r2c_first_prescaled<T>(p[0][q], buf3[0][xr(H - k)], w);
-        x1 = r2c_first_prescaled<T>(p[1][q], buf3[1][xr(H - k)], w);
+        if constexpr (sizeof(T) == 8 && FF_TWIDDLE_FMA) {
+          x0 = r2c_first_prescaled_fma<T>(p[0][q], buf3[0][xr(H - k)], w);
+          x1 = r2c_first_prescaled_fma<T>(p[1][q], buf3[1][xr(H - k)], w);
+        } else {
+          x0 = r2c_first_prescaled<T>(p[0][q], buf3[0][xr(H - k)], w);
+          x1 = r2c_first_prescaled<T>(p[1][q], buf3[1][xr(H - k)], w);
+        }
       }
       q0[k] = x0;
       q1[k] = x1;
@@ -730,16 +737,12 @@ __device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, 
   }
 }
 
-__device__ __forceinline__ float mul_nc(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double mul_nc(double a, double b) { return __dmul_rn(a, b); }
-
 // Pass C split by field: work item (tile, f) transforms field f of the tile's kept
-// columns and forms its part of the flux, -i k_f F_f (k_0 = kr, k_1 = l), each product
-// rounded on its own.  The first of the two items to finish leaves its part in its Q
+// columns.  The first of the two items to finish leaves its transform F_f in its Q
 // columns; the second (an atomic arrival count per tile tells them apart, and resets it)
-// adds the two parts, which gives the same sum whichever field came second, and runs the
-// epilogue.  Nothing waits: twice as many items as column tiles balance a grid that has
-// only a few kept columns per SM.
+// forms N = -i (kr F_0 + l F_1) from its own transform and the other's, by one formula
+// whichever field came second, and runs the epilogue.  Nothing waits: twice as many items
+// as column tiles balance a grid that has only a few kept columns per SM.
 template <typename T, int NY, int EPI>
 __device__ __forceinline__ void vort_c_split(const VortProb<T>& P, const EpiScalars<T>& S, int tile, int f,
                                              cx<T>* smem) {
@@ -757,16 +760,6 @@ __device__ __forceinline__ void vort_c_split(const VortProb<T>& P, const EpiScal
   for (int q = 0; q < 8; ++q) v[0][q] = c < nkd ? __ldcg(mine + (t + q * PP) * P.nkp) : czero<T>();
   cx<T>* const buf[1] = {smem};
   regfft<T, 1, NY, -1>(v, t, P.twy, buf, XCol{tl, ln});
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int j = t + q * PP;
-    cx<T> part = czero<T>();
-    if (c < nkd && (j < la || j >= lb)) {
-      const T k = f == 0 ? P.kr[c] : P.l[j];
-      part = mul_mi(mk<T>(mul_nc(v[0][q].x, k), mul_nc(v[0][q].y, k)));
-    }
-    v[0][q] = part;
-  }
   if (c < nkd) {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -788,7 +781,11 @@ __device__ __forceinline__ void vort_c_split(const VortProb<T>& P, const EpiScal
   for (int q = 0; q < 8; ++q) {
     const int j = t + q * PP;
     N[q] = czero<T>();
-    if (c < nkd && (j < la || j >= lb)) N[q] = add(v[0][q], __ldcg(other + j * P.nkp));
+    if (c < nkd && (j < la || j >= lb)) {
+      const cx<T> o = __ldcg(other + j * P.nkp);
+      const cx<T> f0 = f == 0 ? v[0][q] : o, f1 = f == 0 ? o : v[0][q];
+      N[q] = mul_mi(add(scl(f0, P.kr[c]), scl(f1, P.l[j])));
+    }
   }
   if (c < P.nkr) epilogue_col<T, NY, EPI>(P, S, c, t, N, next);
 }

@@ -320,9 +320,9 @@ int ff_vort_set_config(ff_vort* h, int tla, int tlc, int tlr, int radix_variant)
  * two work items per kept column tile, one per transformed field, the second to finish
  * running the epilogue; for grids with few kept column tiles per SM.  mode -1 lets the
  * library decide from the tile count (the default), 0 and 1 turn it off and on;
- * get_split reports whether the current geometry uses it.  The sums it forms round each
- * field's part separately, so its results may differ from the unsplit form's in the last
- * bit. */
+ * get_split reports whether the current geometry uses it.  It forms the flux by the
+ * unsplit form's formula in another kernel, whose compiled arithmetic may round
+ * differently in the last bit. */
 int ff_vort_set_split(ff_vort* h, int mode);
 int ff_vort_get_split(const ff_vort* h, int32_t* on);
 

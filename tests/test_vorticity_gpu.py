@@ -232,11 +232,11 @@ def test_autotune_keeps_results(ff, cuda):
 @pytest.mark.parametrize("stepper", ["ETDRK4", "FilteredETDRK4", "RK4", "LSRK54", "FilteredLSRK54"])
 def test_split_pass_c_matches_unsplit(ff, cuda, stepper):
     """FP64 pass C split by field (two work items per kept column tile; the second to
-    finish adds the two flux parts and runs the epilogue) against the unsplit form and the
-    oracle, at one, two and four columns per tile (the last kept tile then also holds
-    aliased columns).  The two forms round the flux sum differently, so they agree to
-    rounding, not bit for bit.  Twenty graph replays from the same state give the same
-    result each time: the arrival counters are reset by every launch."""
+    finish forms the flux from both transforms and runs the epilogue) against the unsplit
+    form and the oracle, at one, two and four columns per tile (the last kept tile then
+    also holds aliased columns).  The two forms' kernels may round the flux differently, so
+    they are compared to rounding, not bit for bit.  Twenty graph replays from the same
+    state give the same result each time: the arrival counters are reset by every launch."""
     prob, oprob = make_pair(ff, 128, stepper, ny=64)  # power-of-two lengths: the register path
     fs = prob.timestepper._native(prob.eqn).ensure(prob.sol, prob.clock)
     start = prob.sol.clone()
