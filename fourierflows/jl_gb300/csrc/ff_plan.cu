@@ -60,6 +60,26 @@ static void twiddle(long double e, long double n, double& re, double& im) {
 void host_twiddles(int n, std::vector<double>& t) {
   t.resize(2 * (size_t)n);
   for (int e = 0; e < n; ++e) twiddle(e, n, t[2 * e], t[2 * e + 1]);
+  // For the register-resident FFT of a power-of-two length 16..4096, the twiddles of each
+  // radix-8 stage of span NS > 1 follow, stage by stage and r-major: entry
+  // n + (NS - R0) + (r - 1) NS + k = W_n^(k r n / (8 NS)), r = 1..7, k < NS, where R0 is the
+  // first stage's radix (the spans are R0, 8 R0, ..., n/8; see ff_regfft.cuh).  A warp's
+  // threads then read consecutive entries of one stage and r.
+  if (n >= 16 && n <= 4096 && (n & (n - 1)) == 0) {
+    int L = 0;
+    while ((1 << L) < n) ++L;
+    const int R0 = (L % 3) ? (1 << (L % 3)) : 8;
+    for (int NS = R0; NS * 8 <= n; NS *= 8) {
+      const int tws = n / (NS * 8);
+      for (int r = 1; r < 8; ++r)
+        for (int k = 0; k < NS; ++k) {
+          double re, im;
+          twiddle((long double)k * r * tws, n, re, im);
+          t.push_back(re);
+          t.push_back(im);
+        }
+    }
+  }
 }
 
 void host_real_twiddles(int N, std::vector<double>& t) {

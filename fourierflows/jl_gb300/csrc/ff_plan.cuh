@@ -13,7 +13,8 @@ namespace ff {
 bool factorize(int n, LinePlan& P);
 
 // tw[e] = exp(-2 pi i e / n), e in [0, n), rounded from long-double values; host copy.
-void host_twiddles(int n, std::vector<double>& re_im);  // 2n doubles
+// W_n^e for e < n, then (power-of-two n, 16..4096) the register FFT's stage-major twiddles
+void host_twiddles(int n, std::vector<double>& re_im);
 // W_N^k for k in [0, N/2]: the packing twiddles of a length-N real transform.
 void host_real_twiddles(int N, std::vector<double>& re_im);  // 2 (N/2 + 1) doubles
 

@@ -35,14 +35,19 @@ struct XRow {
   __device__ __forceinline__ int operator()(int p) const { return base + p + (p >> sh); }
 };
 
-// twiddles W_N^(k r TWS), r = 1..7, of a radix-8 stage of span NS > 1 (k = t mod NS): the
-// only stages with twiddles, since a smaller radix only ever opens a transform
+// twiddles W_N^(k r N/(8 NS)), r = 1..7, of a radix-8 stage of span NS > 1 (k = t mod NS):
+// the only stages with twiddles, since a smaller radix only ever opens a transform.  The
+// table holds W_N^e for e < N and then these stage by stage, r-major (host_twiddles):
+// entry N + (NS - R0) + (r - 1) NS + k, R0 the first stage's radix, so consecutive threads
+// read consecutive entries.
 template <typename T, int N, int NS>
 __device__ __forceinline__ void stage_twiddles(int t, const cx<T>* __restrict__ tw, cx<T> (&w)[8]) {
-  constexpr int TWS = N / (NS * 8);
+  constexpr int L = ilog2c(N);
+  constexpr int R0 = (L % 3) != 0 ? (1 << (L % 3)) : 8;
   const int k = t & (NS - 1);
+  const cx<T>* stage = tw + N + (NS - R0);
 #pragma unroll
-  for (int r = 1; r < 8; ++r) w[r] = __ldg(&tw[k * r * TWS]);
+  for (int r = 1; r < 8; ++r) w[r] = __ldg(&stage[(r - 1) * NS + k]);
 }
 
 // one stage of span NS with its twiddles w already in registers; the next stage's
