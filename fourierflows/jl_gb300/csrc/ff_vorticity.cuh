@@ -561,34 +561,79 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
   // conj(A) and W^(H-k) = -conj(W^k).  Partner values go through shared memory; Z[0] and
   // the self-paired Z[H/2] are formed directly.
   cx<T> v[3][8];
+  if constexpr (sizeof(T) == 4) {
+    // FP32: every load of the row first, then the packing.  (Loads placed after the
+    // shared-memory stores of the previous field wait behind them: one memory round trip
+    // per field and pair, and this latency-bound pass took 19% longer.)
+    cx<T> xa[3][4], xb[3][4], wk[4];
 #pragma unroll
-  for (int f = 0; f < 3; ++f) {
-    const cx<T>* src = P.W + f * fstride + j * nkp;
+    for (int q = 0; q < 4; ++q) wk[q] = __ldg(&P.rtw[t + q * PP]);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int k = t + q * PP;
-      cx<T> zk = czero<T>(), zh = czero<T>();
-      if (j < ny) {
-        const cx<T> xk = k < nkd ? src[k] : czero<T>();
-        const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
-        if (k == 0) {
-          zk = c2r_pre<T>(xk, xh, __ldg(&P.rtw[0]), 0);
-        } else if constexpr (sizeof(T) == 8 && FF_TWIDDLE_FMA) {
-          c2r_pair_fma<T>(xk, xh, __ldg(&P.rtw[k]), zk, zh);
-        } else {
-          const cx<T> b = conj(xh);
-          const cx<T> a = add(xk, b);
-          const cx<T> pp = cmulc(sub(xk, b), __ldg(&P.rtw[k]));
-          zk = add(a, mul_i(pp));
-          zh = mk<T>(a.x + pp.y, pp.x - a.y);
-        }
+    for (int f = 0; f < 3; ++f) {
+      const cx<T>* src = P.W + f * fstride + j * nkp;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = t + q * PP;
+        xa[f][q] = (j < ny && k < nkd) ? src[k] : czero<T>();
+        xb[f][q] = (j < ny && (H - k) < nkd) ? src[H - k] : czero<T>();
       }
-      v[f][q] = zk;
-      if (k != 0) buf3[f][xr(H - k)] = zh;
     }
-    if (t == 0) {
-      const cx<T> xm = (j < ny && H / 2 < nkd) ? src[H / 2] : czero<T>();
-      buf3[f][xr(H / 2)] = j < ny ? c2r_pre<T>(xm, xm, __ldg(&P.rtw[H / 2]), H / 2) : czero<T>();
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = t + q * PP;
+        cx<T> zk = czero<T>(), zh = czero<T>();
+        if (j < ny) {
+          const cx<T> xk = xa[f][q], xh = xb[f][q];
+          if (k == 0) {
+            zk = c2r_pre<T>(xk, xh, wk[0], 0);
+          } else {
+            const cx<T> b = conj(xh);
+            const cx<T> a = add(xk, b);
+            const cx<T> pp = cmulc(sub(xk, b), wk[q]);
+            zk = add(a, mul_i(pp));
+            zh = mk<T>(a.x + pp.y, pp.x - a.y);
+          }
+        }
+        v[f][q] = zk;
+        if (k != 0) buf3[f][xr(H - k)] = zh;
+      }
+      if (t == 0) {
+        const cx<T> xm = (j < ny && H / 2 < nkd) ? P.W[f * fstride + j * nkp + H / 2] : czero<T>();
+        buf3[f][xr(H / 2)] = j < ny ? c2r_pre<T>(xm, xm, __ldg(&P.rtw[H / 2]), H / 2) : czero<T>();
+      }
+    }
+  } else {
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const cx<T>* src = P.W + f * fstride + j * nkp;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = t + q * PP;
+        cx<T> zk = czero<T>(), zh = czero<T>();
+        if (j < ny) {
+          const cx<T> xk = k < nkd ? src[k] : czero<T>();
+          const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
+          if (k == 0) {
+            zk = c2r_pre<T>(xk, xh, __ldg(&P.rtw[0]), 0);
+          } else if constexpr (FF_TWIDDLE_FMA) {
+            c2r_pair_fma<T>(xk, xh, __ldg(&P.rtw[k]), zk, zh);
+          } else {
+            const cx<T> b = conj(xh);
+            const cx<T> a = add(xk, b);
+            const cx<T> pp = cmulc(sub(xk, b), __ldg(&P.rtw[k]));
+            zk = add(a, mul_i(pp));
+            zh = mk<T>(a.x + pp.y, pp.x - a.y);
+          }
+        }
+        v[f][q] = zk;
+        if (k != 0) buf3[f][xr(H - k)] = zh;
+      }
+      if (t == 0) {
+        const cx<T> xm = (j < ny && H / 2 < nkd) ? src[H / 2] : czero<T>();
+        buf3[f][xr(H / 2)] = j < ny ? c2r_pre<T>(xm, xm, __ldg(&P.rtw[H / 2]), H / 2) : czero<T>();
+      }
     }
   }
   __syncthreads();
@@ -617,6 +662,43 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
     buf3[1][xr(t + q * PP)] = p[1][q];
   }
   __syncthreads();
+  if constexpr (sizeof(T) == 4) {
+    // FP32: every unpacked value first, then the stores (a load placed after a store to Q
+    // would wait behind it)
+    if (j < ny) {
+      cx<T>* q0 = P.Q + j * P.nkp;
+      cx<T>* q1 = q0 + fstride;
+      cx<T> x0[8], x1[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = t + q * PP;
+        if (k == 0) {
+          const cx<T> z0 = p[0][0], z1 = p[1][0];
+          x0[q] = mk<T>((z0.x + z0.y) * T(2), T(0));
+          x1[q] = mk<T>((z1.x + z1.y) * T(2), T(0));
+        } else {
+          const cx<T> w = __ldg(&P.rtw[k < nkd ? k : 0]);
+          x0[q] = r2c_first_prescaled<T>(p[0][q], buf3[0][xr(H - k)], w);
+          x1[q] = r2c_first_prescaled<T>(p[1][q], buf3[1][xr(H - k)], w);
+        }
+      }
+      if (t == 0 && nkd > H) {  // no dealiasing: the Nyquist column too
+        const cx<T> z0 = p[0][0], z1 = p[1][0];
+        q0[H] = mk<T>((z0.x - z0.y) * T(2), T(0));
+        q1[H] = mk<T>((z1.x - z1.y) * T(2), T(0));
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = t + q * PP;
+        if (k < nkd) {
+          q0[k] = x0[q];
+          q1[k] = x1[q];
+        }
+      }
+    }
+    __syncthreads();
+    return;
+  }
   if (j < ny) {
     cx<T>* q0 = P.Q + j * P.nkp;
     cx<T>* q1 = q0 + fstride;
