@@ -197,7 +197,7 @@ NCU = {
     "fp32_batch4_1024": {
         "capture": "ncu --set full on bench.py --profile-case batch --tiles 4,4,1: 4 x 1024^2 FP32, "
                    "passes A, B and C of step 2",
-        "A": {"dram_bytes": 9.09e6}, "B": {"dram_bytes": 33.84e6}, "C": {"dram_bytes": 35.57e6},
+        "A": {"dram_bytes": 9.16e6}, "B": {"dram_bytes": 33.85e6}, "C": {"dram_bytes": 35.44e6},
     },
 }
 
