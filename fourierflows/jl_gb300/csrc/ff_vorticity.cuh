@@ -605,6 +605,8 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
       }
     }
   } else {
+    // FP64: too few registers to hold the row; read-only global loads (W is not written
+    // during this pass), which the compiler may move ahead of the shared-memory stores
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
       const cx<T>* src = P.W + f * fstride + j * nkp;
@@ -613,8 +615,8 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
         const int k = t + q * PP;
         cx<T> zk = czero<T>(), zh = czero<T>();
         if (j < ny) {
-          const cx<T> xk = k < nkd ? src[k] : czero<T>();
-          const cx<T> xh = (H - k) < nkd ? src[H - k] : czero<T>();
+          const cx<T> xk = k < nkd ? __ldg(src + k) : czero<T>();
+          const cx<T> xh = (H - k) < nkd ? __ldg(src + H - k) : czero<T>();
           if (k == 0) {
             zk = c2r_pre<T>(xk, xh, __ldg(&P.rtw[0]), 0);
           } else if constexpr (FF_TWIDDLE_FMA) {
@@ -631,7 +633,7 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
         if (k != 0) buf3[f][xr(H - k)] = zh;
       }
       if (t == 0) {
-        const cx<T> xm = (j < ny && H / 2 < nkd) ? src[H / 2] : czero<T>();
+        const cx<T> xm = (j < ny && H / 2 < nkd) ? __ldg(src + H / 2) : czero<T>();
         buf3[f][xr(H / 2)] = j < ny ? c2r_pre<T>(xm, xm, __ldg(&P.rtw[H / 2]), H / 2) : czero<T>();
       }
     }
@@ -725,8 +727,9 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
           x1 = r2c_first_prescaled<T>(p[1][q], buf3[1][xr(H - k)], w);
         }
       }
-      q0[k] = x0;
-      q1[k] = x1;
+      // global-space stores: the shared-memory loads of the next pair need not wait
+      __stcg(q0 + k, x0);
+      __stcg(q1 + k, x1);
     }
   }
   __syncthreads();
