@@ -301,15 +301,17 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
     }
     return in;
   }
+  // ETDRK4 substeps 1-3 only read these arrays (read-only loads, which may move ahead of
+  // the shared-memory traffic of the transforms)
   if (EPI == EPI_ETD1 || EPI == EPI_ETD2) {
-    in.x = P.sol[e];
-    in.a = P.eh[e];
-    in.b = P.zc[e];
+    in.x = __ldg(P.sol + e);
+    in.a = __ldg(P.eh + e);
+    in.b = __ldg(P.zc + e);
   } else if (EPI == EPI_ETD3) {
-    in.x = FUSED ? P.sol[e] : P.s1[e];
-    in.n1 = P.n1[e];
-    in.a = P.eh[e];
-    in.b = P.zc[e];
+    in.x = FUSED ? __ldg(P.sol + e) : __ldg(P.s1 + e);
+    in.n1 = __ldg(P.n1 + e);
+    in.a = __ldg(P.eh + e);
+    in.b = __ldg(P.zc + e);
   } else if (EPI == EPI_ETD4) {
     in.x = P.sol[e];
     in.n1 = P.n1[e];
@@ -783,8 +785,8 @@ __device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, 
       T ik = T(0), lj = T(0);
       if (c < nkd && (j < la || j >= lb)) {
         z = x[q];
-        ik = P.invK[c + j * nkr];
-        lj = P.l[j];
+        ik = __ldg(P.invK + c + j * nkr);
+        lj = __ldg(P.l + j);
       }
       v[0][q] = mul_i(scl(z, lj * ik));
       v[1][q] = mul_mi(scl(z, kc * ik));
