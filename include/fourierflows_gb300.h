@@ -269,8 +269,10 @@ int ff_vort_calcN(ff_vort* h, int64_t prob, const void* sol, void* N, void* stre
  * synchronises the device, so not during stream capture); calcN_slot launches the three
  * passes of a bound slot with no host staging, so it can be captured in a CUDA graph (a
  * checkpointed adjoint replays one per step).  A later set_config, set_split or autotune
- * invalidates the slots: calcN_slot then fails until they are bound again.  The same
- * serialisation rule as ff_vort_calcN applies (the handle's workspace). */
+ * invalidates the slots: calcN_slot then fails until they are bound again.  Binding a slot
+ * again frees its previous staging buffer, so a CUDA graph that captured calcN_slot on it
+ * must not be replayed after that.  The same serialisation rule as ff_vort_calcN applies
+ * (the handle's workspace). */
 #define FF_VORT_CALC_SLOTS 16
 int ff_vort_calcN_bind(ff_vort* h, int slot, int64_t prob, const void* sol, void* N);
 int ff_vort_calcN_slot(ff_vort* h, int slot, void* stream);
