@@ -313,14 +313,15 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
     in.a = __ldg(P.eh + e);
     in.b = __ldg(P.zc + e);
   } else if (EPI == EPI_ETD4) {
+    // sol is rewritten by this pass; N1..N3 and the coefficients are only read
     in.x = P.sol[e];
-    in.n1 = P.n1[e];
-    in.n2 = P.n2[e];
-    in.n3 = P.n3[e];
-    in.a = P.eL[e];
-    in.b = P.al[e];
-    in.c = P.be[e];
-    in.d = P.ga[e];
+    in.n1 = __ldg(P.n1 + e);
+    in.n2 = __ldg(P.n2 + e);
+    in.n3 = __ldg(P.n3 + e);
+    in.a = __ldg(P.eL + e);
+    in.b = __ldg(P.al + e);
+    in.c = __ldg(P.be + e);
+    in.d = __ldg(P.ga + e);
   } else if (EPI == EPI_RK1 || EPI == EPI_LS) {
     in.x = P.sol[e];
     in.a = P.L[e];
