@@ -323,21 +323,23 @@ __device__ __forceinline__ EpiIn<T> epi_load(const VortProb<T>& P, const EpiScal
     in.c = __ldg(P.be + e);
     in.d = __ldg(P.ga + e);
   } else if (EPI == EPI_RK1 || EPI == EPI_LS) {
-    in.x = P.sol[e];
-    in.a = P.L[e];
+    // RK1 writes only N1 and the stage state; an LSRK54 stage rewrites sol and S2
+    in.x = EPI == EPI_RK1 ? __ldg(P.sol + e) : P.sol[e];
+    in.a = __ldg(P.L + e);
     if (EPI == EPI_LS && !S.first) in.n1 = P.s1[e];
   } else if (EPI == EPI_RK2 || EPI == EPI_RK3) {
-    in.x = P.s1[e];
-    in.n1 = P.sol[e];
-    in.a = P.L[e];
+    in.x = P.s1[e];  // rewritten by this pass
+    in.n1 = __ldg(P.sol + e);
+    in.a = __ldg(P.L + e);
   } else if (EPI == EPI_RK4) {
-    in.x = P.s1[e];
-    in.n1 = P.n1[e];
-    in.n2 = P.n2[e];
-    in.n3 = P.n3[e];
-    in.a = P.L[e];
+    // sol is rewritten by this pass; the stage state, N1..N3 and L are only read
+    in.x = __ldg(P.s1 + e);
+    in.n1 = __ldg(P.n1 + e);
+    in.n2 = __ldg(P.n2 + e);
+    in.n3 = __ldg(P.n3 + e);
+    in.a = __ldg(P.L + e);
   }
-  if ((EPI == EPI_ETD4 || EPI == EPI_RK4 || EPI == EPI_LS) && S.use_filter) in.fl = P.filter[e];
+  if ((EPI == EPI_ETD4 || EPI == EPI_RK4 || EPI == EPI_LS) && S.use_filter) in.fl = __ldg(P.filter + e);
   return in;
 }
 
