@@ -176,7 +176,7 @@ def pass_bytes(n, es, fused_a, filtered=False):
     return {"A": a_in + a_out, "B": b, "C1": c[1], "C2": c[2], "C3": c[3], "C4": c[4], "step": step}
 
 
-def survey_step_bytes(n, s):
+def model_step_bytes(n, s):
     """The scope table's model of an ETDRK4 step: 20 (C + R) + 21 C with C = (n/2+1) n 2 s and
     R = n^2 s (one read + one write per unfused 2D FFT, operands of the four combinations
     read once)."""
@@ -306,8 +306,8 @@ def fp64_roofline(ff, tA, tB, tC, steps_per_s, hbm, peak_src):
            "hbm": {"achieved": hbm_gbs, "peak": hbm, "unit": "GB/s", "frac": hbm_gbs / hbm,
                    "peak_source": peak_src, "bytes_per_launch": byts["B"]},
            "step_bytes": byts["step"], "step_hbm_frac": byts["step"] * steps_per_s / 1e9 / hbm,
-           "step_survey_bytes": survey_step_bytes(N, 8),
-           "step_survey_frac": survey_step_bytes(N, 8) * steps_per_s / 1e9 / hbm}
+           "step_model_bytes": model_step_bytes(N, 8),
+           "step_model_frac": model_step_bytes(N, 8) * steps_per_s / 1e9 / hbm}
     return out
 
 
@@ -381,7 +381,7 @@ def our_arm(a):
                 "config": {"workload": WORKLOAD, "global_batch": world, "parallelism": f"replicas{world}",
                            "l2": "flushed between steps (256 MiB write)", "tiles": cfg64,
                            "algorithmic_bytes_per_step": roofline["step_bytes"],
-                           "survey_bytes_per_step": survey_step_bytes(N, 8)},
+                           "model_bytes_per_step": model_step_bytes(N, 8)},
                 "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "forms": forms}
@@ -446,7 +446,7 @@ def run_forms(torch, ff, a, hbm, peak_src, fused_fp64):
     dom = max(passes, key=lambda k: passes[k][0])
     ach = passes[dom][1] / (passes[dom][0] * 1e-3) / 1e9
     step_ach = B * bts["step"] / (msb * 1e-3) / 1e9
-    step_sv = B * survey_step_bytes(N, 4) / (msb * 1e-3) / 1e9
+    step_md = B * model_step_bytes(N, 4) / (msb * 1e-3) / 1e9
     cap = NCU["fp32_batch4_1024"]
     out["fp32_batched_1024x32"] = {
         "value": B * 1e3 / msb, "unit": "problem-steps/s (1024^2 ETDRK4)", "ms_per_step": msb,
@@ -459,8 +459,8 @@ def run_forms(torch, ff, a, hbm, peak_src, fused_fp64):
                      "kernel": f"k_vort_{dom.lower()}_r<float> (pass {dom})", "peak_source": peak_src,
                      "bytes_per_launch": passes[dom][1], "pass_ms": {"A": tA, "B": tB, "C": tC}},
         "step_bytes_per_problem": bts["step"], "step_algorithmic_gbs": step_ach, "step_frac": step_ach / hbm,
-        "step_survey_bytes_per_problem": survey_step_bytes(N, 4),
-        "step_survey_gbs": step_sv, "step_survey_frac": step_sv / hbm, **acc}
+        "step_model_bytes_per_problem": model_step_bytes(N, 4),
+        "step_model_gbs": step_md, "step_model_frac": step_md / hbm, **acc}
     del ens, saved
     # the uneven ensemble: 128 x 128^2, 128 x 256^2, 96 x 512^2, 32 x 1024^2, nu log-uniform
     u = ff.Vorticity.uniform01(99, 384)
@@ -477,7 +477,7 @@ def run_forms(torch, ff, a, hbm, peak_src, fused_fp64):
     msu = timed_steps(torch, ens.fs, bsteps, flush) / bsteps
     gp = ens.grid_points
     ubytes = sum(pass_bytes(n, 8, fused_a=True)["step"] for n, _, _ in spec)
-    usurvey = sum(survey_step_bytes(n, 4) for n, _, _ in spec)
+    umodel = sum(model_step_bytes(n, 4) for n, _, _ in spec)
     ugbs = ubytes / (msu * 1e-3) / 1e9
     out["ensemble_uneven_384"] = {"value": 384 * 1e3 / msu, "unit": "problem-steps/s", "ms_per_step": msu,
                                   "tiles": ens.fs.config(),
@@ -486,8 +486,8 @@ def run_forms(torch, ff, a, hbm, peak_src, fused_fp64):
                                   "roofline": {"bound": "hbm", "achieved": ugbs, "peak": hbm, "unit": "GB/s",
                                                "frac": ugbs / hbm, "kernel": "whole step (9 launches)",
                                                "bytes_per_step": ubytes, "peak_source": peak_src,
-                                               "survey_bytes_per_step": usurvey,
-                                               "survey_frac": usurvey / (msu * 1e-3) / 1e9 / hbm}}
+                                               "model_bytes_per_step": umodel,
+                                               "model_frac": umodel / (msu * 1e-3) / 1e9 / hbm}}
     del ens
     out["diffusion3d_64x128^3"] = diffusion3d_ensemble(torch, ff, a, hbm, peak_src, flush)
     out["precision_2048"] = precision_2048(torch, ff)
