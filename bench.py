@@ -177,9 +177,9 @@ def pass_bytes(n, es, fused_a, filtered=False):
 
 
 def model_step_bytes(n, s):
-    """The scope table's model of an ETDRK4 step: 20 (C + R) + 21 C with C = (n/2+1) n 2 s and
-    R = n^2 s (one read + one write per unfused 2D FFT, operands of the four combinations
-    read once)."""
+    """Bytes of an unfused ETDRK4 step of the vorticity problem: 20 (C + R) + 21 C with
+    C = (n/2+1) n 2 s and R = n^2 s (one read and one write per 2D FFT, the operands of the
+    four combinations read once)."""
     C = (n // 2 + 1) * n * 2 * s
     R = n * n * s
     return 20 * (C + R) + 21 * C
