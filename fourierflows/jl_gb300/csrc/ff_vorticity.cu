@@ -3,6 +3,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -200,6 +202,7 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
   std::vector<WorkItem> wa, wb, wc;
   const size_t es = elem<T>();
   int64_t woff = 0, coff = 0;
+  std::map<std::tuple<const void*, const void*, int, int>, const void*> scaled;
   if (h->d_cnt) { cudaFree(h->d_cnt); h->d_cnt = nullptr; }
   if (geom.split_c) {
     int64_t tiles = 0;
@@ -242,6 +245,27 @@ template <typename T> int build(ff_vort* h, const Geom& geom) {
     P.kr = (const T*)q.kr;
     P.l = (const T*)q.l;
     P.invK = (const T*)q.invKrsq;
+    if (geom.reg) {
+      // kr and l times scale2 / 2 (a power of two: exact), one table per distinct
+      // (kr, l, size) among the problems
+      const auto key = std::make_tuple(q.kr, q.l, P.nx, P.ny);
+      auto hit = scaled.find(key);
+      if (hit == scaled.end()) {
+        std::vector<T> kr(P.nkr), l(P.ny);
+        FF_CUDA(cudaMemcpy(kr.data(), q.kr, kr.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        FF_CUDA(cudaMemcpy(l.data(), q.l, l.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        const double ps = 0.5 * s * s;
+        std::vector<double> ts;
+        for (T x : kr) ts.push_back((double)x * ps);
+        for (T x : l) ts.push_back((double)x * ps);
+        if (ts.size() % 2) ts.push_back(0.0);  // the table uploads (re, im) pairs
+        if (int st = upload_table(ts, sizeof(T) == 8 ? FF_F64 : FF_F32, &d)) return st;
+        h->tables.push_back(d);
+        hit = scaled.emplace(key, (const void*)d).first;
+      }
+      P.krs = (const T*)hit->second;
+      P.ls = P.krs + P.nkr;
+    }
     P.W = (cx<T>*)h->d_W + woff * 3;
     P.Q = (cx<T>*)h->d_Q + woff * 2;
     woff += (int64_t)P.nkp * P.ny;

@@ -67,7 +67,7 @@ template <typename T> struct VortProb {
   int nx, ny, nkr, nkd;  // nkd: kept kr columns [0, nkd)
   int la, lb;            // aliased l rows [la, lb)
   int nkp, pad0;         // row pitch of W and Q: nkd rounded up to 16 bytes
-  T scale2;              // 1 / (nx ny)^2, applied to each physical product
+  T scale2;              // 1 / (nx ny)^2, applied to each physical product (generic path)
   LinePlan Px, Py;       // length nx/2 and ny
   const cx<T>* twx;
   const cx<T>* twy;
@@ -75,6 +75,11 @@ template <typename T> struct VortProb {
   const T* kr;           // nkr
   const T* l;            // ny
   const T* invK;         // nkr * ny, 1/K^2 with the mean mode 0
+  // register path: kr (nkr) and l (ny) times the product scale scale2 / 2, a power of two
+  // there, for the velocities of pass A, so that pass B's products u zeta and v zeta come
+  // out scaled without a multiply of their own (bit for bit the products scaled after)
+  const T* krs;
+  const T* ls;
   cx<T>* W;              // 3 * nkp * ny
   cx<T>* Q;              // 2 * nkp * ny
   // stepper state (nkr * ny each)
@@ -484,7 +489,7 @@ __device__ __forceinline__ void vort_a_reg3(const VortProb<T>& P, const cx<T>* _
   const int ln = threadIdx.x & (tl - 1), t = threadIdx.x / tl;
   const int c = tile * tl + ln;
   const int nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb;
-  const T kc = c < nkd ? P.kr[c] : T(0);
+  const T kc = c < nkd ? P.krs[c] : T(0);
   cx<T> v[3][8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
@@ -495,10 +500,10 @@ __device__ __forceinline__ void vort_a_reg3(const VortProb<T>& P, const cx<T>* _
       const int e = c + j * nkr;
       s = zh[e];
       ik = P.invK[e];
-      lj = P.l[j];
+      lj = P.ls[j];
     }
-    v[0][q] = mul_i(scl(s, lj * ik));   // u_hat = i l zeta_hat / K^2
-    v[1][q] = mul_mi(scl(s, kc * ik));  // v_hat = -i kr zeta_hat / K^2
+    v[0][q] = mul_i(scl(s, lj * ik));   // u_hat = i l zeta_hat / K^2 (scaled)
+    v[1][q] = mul_mi(scl(s, kc * ik));  // v_hat = -i kr zeta_hat / K^2 (scaled)
     v[2][q] = s;
   }
   const int bsz = (NY + NY / 8) * tl;
@@ -530,8 +535,8 @@ __device__ __forceinline__ void vort_a_reg(const VortProb<T>& P, const cx<T>* __
     if (c < nkd && (j < la || j >= lb)) {
       const int e = c + j * nkr;
       const cx<T> s = zh[e];
-      if (f == 0) z = mul_i(scl(s, P.l[j] * P.invK[e]));
-      else if (f == 1) z = mul_mi(scl(s, P.kr[c] * P.invK[e]));
+      if (f == 0) z = mul_i(scl(s, P.ls[j] * P.invK[e]));
+      else if (f == 1) z = mul_mi(scl(s, P.krs[c] * P.invK[e]));
       else z = s;
     }
     v[0][q] = z;
@@ -650,15 +655,14 @@ __device__ __forceinline__ void vort_b_reg(const VortProb<T>& P, int tile, cx<T>
     for (int q = 4; q < 8; ++q) v[f][q] = buf3[f][xr(t + q * PP)];
   __syncthreads();
   regfft<T, 3, H, 1>(v, t, P.twx, buf3, xr);
-  // products u zeta and v zeta in physical space (packed real pairs), normalisation folded
-  // in, and the unpack's two halvings too (s2 / 2: exact, so the unpacked values are those
-  // of the unhalved form bit for bit)
-  const T s2 = P.scale2 * T(0.5);
+  // products u zeta and v zeta in physical space (packed real pairs).  u and v arrive
+  // scaled by scale2 / 2 (pass A's krs and ls): the normalisation and the unpack's two
+  // halvings, a power of two, so the products are those scaled afterwards bit for bit
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const cx<T> z = v[2][q];
-    v[0][q] = mk<T>(v[0][q].x * z.x * s2, v[0][q].y * z.y * s2);
-    v[1][q] = mk<T>(v[1][q].x * z.x * s2, v[1][q].y * z.y * s2);
+    v[0][q] = mk<T>(v[0][q].x * z.x, v[0][q].y * z.y);
+    v[1][q] = mk<T>(v[1][q].x * z.x, v[1][q].y * z.y);
   }
   cx<T>(&p)[2][8] = *reinterpret_cast<cx<T>(*)[2][8]>(&v[0][0]);
   regfft<T, 2, H, -1>(p, t, P.twx, buf3, xr);
@@ -775,7 +779,7 @@ __device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, 
                                             cx<T>* smem) {
   constexpr int PP = NY / 8;
   const int nkr = P.nkr, nkd = P.nkd, la = P.la, lb = P.lb;
-  const T kc = c < nkd ? P.kr[c] : T(0);
+  const T kc = c < nkd ? P.krs[c] : T(0);
   const int bsz = (NY + NY / 8) * tl;
   const int fs = P.nkp * P.ny;
   cx<T>* Wc = P.W + c;
@@ -789,7 +793,7 @@ __device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, 
       if (c < nkd && (j < la || j >= lb)) {
         z = x[q];
         ik = __ldg(P.invK + c + j * nkr);
-        lj = __ldg(P.l + j);
+        lj = __ldg(P.ls + j);
       }
       v[0][q] = mul_i(scl(z, lj * ik));
       v[1][q] = mul_mi(scl(z, kc * ik));
@@ -813,7 +817,7 @@ __device__ __forceinline__ void a_from_regs(const VortProb<T>& P, int c, int t, 
         cx<T> z = czero<T>();
         if (c < nkd && (j < la || j >= lb)) {
           const T ik = P.invK[c + j * nkr];
-          z = f == 0 ? mul_i(scl(x[q], P.l[j] * ik)) : f == 1 ? mul_mi(scl(x[q], kc * ik)) : x[q];
+          z = f == 0 ? mul_i(scl(x[q], P.ls[j] * ik)) : f == 1 ? mul_mi(scl(x[q], kc * ik)) : x[q];
         }
         v[0][q] = z;
       }

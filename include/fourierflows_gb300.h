@@ -249,7 +249,8 @@ typedef struct {
 /* Create a fused stepper for nprob problems (all of precision prec and one stepper kind).
  * `filtered` applies each problem's filter at the end of the step as the Filtered*
  * steppers do (src/timesteppers.jl:279,408,552).  The pointers in probs must stay valid
- * for the handle's lifetime. */
+ * for the handle's lifetime.  kr and l are read once here (and again by set_split and
+ * autotune) into scaled copies: like the grid they come from, they must not change. */
 int ff_vort_create(int prec, int stepper, int filtered, double dt, int64_t nprob, const ff_vort_problem* probs,
                    ff_vort** out);
 int ff_vort_destroy(ff_vort* h);
