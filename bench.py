@@ -197,7 +197,7 @@ NCU = {
     "fp32_batch4_1024": {
         "capture": "ncu --set full on bench.py --profile-case batch --tiles 4,4,1: 4 x 1024^2 FP32, "
                    "passes A, B and C of step 2",
-        "A": {"dram_bytes": 9.14e6}, "B": {"dram_bytes": 33.84e6}, "C": {"dram_bytes": 35.20e6},
+        "A": {"dram_bytes": 9.13e6}, "B": {"dram_bytes": 33.83e6}, "C": {"dram_bytes": 35.35e6},
     },
 }
 
